@@ -1,0 +1,282 @@
+#!/usr/bin/env python3
+"""Throughput of the EA-LCD-MC hot path on one GB300 (spin updates per picosecond).
+
+Workload (one job, reference layout): L=24, Lz=192 tube (110,592 sites), OBC
+along z, NB=32 temperatures uniform in T in [0.6, 1.6], NR=8 replicas, 32
+disorder samples; Metropolis + energy + parallel tempering every sweep and a
+Houdayer move on the colder half every 5 sweeps.  One step = 5 x (sweep +
+energy + PT) + 1 Houdayer move = 5 * V * NR * NB * 32 spin updates.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference algorithm on the host cores (the oracle's
+C restatement, all threads) on a bounded sample of the same workload.
+Prints one JSON line (rank 0).
+"""
+import argparse
+import ctypes as C
+import importlib.util
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+L, LZ, NR, NS, HOUFR = 24, 192, 8, 32, 5
+LUT = os.path.join(ROOT, "tests", "golden", "lut_T06_16_N32.npz")
+MASTERS = (0x1234567890ABCDEF, 0x0FEDCBA987654321, 0x1111222233334444, 0x5555666677778888)
+WORKLOAD = "L24_Lz192_OBC_NB32_NR8_ns32_ptfr1_houfr5"
+
+
+def load_eagb():
+    spec = importlib.util.spec_from_file_location("eagb", os.path.join(ROOT, "ea-lcd-mc_gb300", "eagb.py"))
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    return m
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region (SM clock, throttle reasons)."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (self.out or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_sample(nthreads, sweeps=1):
+    """Reference algorithm (oracle C restatement) on host cores: one sample of the
+    bench geometry, `sweeps` Metropolis sweeps.  Returns (spin updates, seconds)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_py as O
+    d = np.load(LUT)
+    sim = O.Sim(L, LZ, d["betas"], d["cum"], nbits=1, NR=NR, bc=O.OBC, masters=MASTERS)
+    t0 = time.perf_counter()
+    it = 0
+    for _ in range(sweeps):
+        for p in (0, 1):
+            ctr = O.fill_bits(sim.prc, sim.xo, NR, it, 0)
+            sim.half_sweep(ctr, p, nthreads)
+            it += 1
+    dt = time.perf_counter() - t0
+    return L * L * LZ * NR * len(d["betas"]) * sweeps, dt
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    n = os.cpu_count() or 1
+    vals = []
+    for i in range(args.warmup + args.steps):
+        su, dt = cpu_sample(n)
+        if i >= args.warmup:
+            vals.append((su, dt))
+    su = sum(v[0] for v in vals)
+    dt = sum(v[1] for v in vals)
+    value = su / dt / 1e12
+    line = {"metric": "spin_updates_per_ps", "value": value, "unit": "spin-updates/ps", "impl": "reference",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic (seeded couplings and spins as the reference generates them)",
+            "config": {"workload": WORKLOAD, "sample": "1 disorder sample x 1 sweep per step"},
+            "cpu_baseline": {"value": value, "unit": "spin-updates/ps", "cores": n, "kind": "port",
+                             "sample": "1 sample x 1 Metropolis sweep of L24 Lz192 NB32 NR8 per step, oracle C restatement, OpenMP"},
+            "e2e": {"value": value, "unit": "spin-updates/ps", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local):
+    import torch
+    eagb = load_eagb()
+    dev = local
+    torch.cuda.set_device(dev)
+    d = np.load(LUT)
+    betas, cum = d["betas"], d["cum"]
+    NB = len(betas)
+    V = L * L * LZ
+    job = eagb.new_job(L, LZ, betas, cum, nsamples=NS, NR=NR, bc=eagb.EA_OBC, masters=MASTERS, device=dev, jobid=rank)
+    stream = torch.cuda.ExternalStream(job.stream(), device=dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.int32, device=dev)   # 512 MB > L2
+    su_step = HOUFR * V * NR * NB * NS
+
+    def step():
+        for _ in range(HOUFR):
+            job.monte_carlo(1)
+            job.parallel_tempering()
+        job.houdayer(0)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        step()
+    job.sync()
+    # timed region: device events on the job's stream, L2 flushed between steps
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier()
+    torch.cuda.synchronize(dev)
+    eagb._ck(eagb.lib().ea_profile(job.ctx, 1))
+    with Clocks(dev) as clk, torch.cuda.stream(stream):
+        for i in range(args.steps):
+            flush.fill_(i)
+            ev[i][0].record(stream)
+            step()
+            ev[i][1].record(stream)
+        job.sync()
+    torch.cuda.synchronize(dev)
+    barrier()
+    ms = sum(a.elapsed_time(b) for a, b in ev)
+    nsw, sw_ms = C.c_int64(), C.c_double()
+    eagb._ck(eagb.lib().ea_kernel_time(job.ctx, 0, C.byref(nsw), C.byref(sw_ms)))
+    npt, pt_ms = C.c_int64(), C.c_double()
+    eagb._ck(eagb.lib().ea_kernel_time(job.ctx, 1, C.byref(npt), C.byref(pt_ms)))
+    ncl, cl_ms = C.c_int64(), C.c_double()
+    eagb._ck(eagb.lib().ea_kernel_time(job.ctx, 2, C.byref(ncl), C.byref(cl_ms)))
+    eagb._ck(eagb.lib().ea_profile(job.ctx, 0))
+
+    # end to end through the C ABI with host buffers: every step uploads the
+    # spin state from pinned memory and reads the energies back
+    half = (L // 4) ** 2 * (LZ // 4) // 2
+    nw = NB * half * NR
+    pinned = [(torch.zeros(nw, dtype=torch.int64).pin_memory(), torch.zeros(nw, dtype=torch.int64).pin_memory())
+              for _ in range(NS)]
+    for s in range(NS):
+        ev_, od_ = job.get_spins(s)
+        pinned[s][0].numpy()[:] = ev_.view(np.int64)
+        pinned[s][1].numpy()[:] = od_.view(np.int64)
+    E_out = np.zeros((NS, NR, NB), np.int32)
+    ne = max(2, args.steps // 2)
+    barrier()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for i in range(ne):
+        for s in range(NS):
+            eagb._ck(eagb.lib().ea_set_spins(job.ctx, s, C.c_void_p(pinned[s][0].data_ptr()),
+                                             C.c_void_p(pinned[s][1].data_ptr())))
+        step()
+        eagb._ck(eagb.lib().ea_measure_energy(job.ctx, eagb.P(E_out)))
+    torch.cuda.synchronize(dev)
+    e2e_s = time.perf_counter() - t0
+    barrier()
+
+    # max over ranks
+    t = torch.tensor([ms, e2e_s], dtype=torch.float64, device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms, e2e_s = float(t[0]), float(t[1])
+    if rank != 0:
+        job.close()
+        return
+    value = world * su_step * args.steps / (ms * 1e-3) / 1e12
+    e2e = world * su_step * ne / e2e_s / 1e12
+    hbm, how = peaks()
+    # algorithmic bytes of one half-sweep launch: read + write every word of the
+    # updated parity, read every word of the other parity once, read the couplings
+    words_parity = NS * NB * half * NR
+    alg_bytes = words_parity * 8 * 3 + NS * 6 * half * 8
+    sweep_ms = sw_ms.value / max(1, nsw.value)
+    achieved = alg_bytes / (sweep_ms * 1e-3) / 1e9
+    line = {
+        "metric": "spin_updates_per_ps", "value": value, "unit": "spin-updates/ps", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic (seeded couplings and spins as the reference generates them)",
+        "config": {"workload": WORKLOAD, "L": L, "Lz": LZ, "nbetas": NB, "nrep": NR, "nsamples": NS,
+                   "bc": "OBC", "ptfr": 1, "houfr": HOUFR, "form": "plain (one job per launch)",
+                   "l2": "flushed between steps (512 MB write)", "parallelism": "replicas" if world > 1 else "single"},
+        "e2e": {"value": e2e, "unit": "spin-updates/ps", "h2d_bytes_per_step": NS * 2 * nw * 8,
+                "d2h_bytes_per_step": NS * NR * NB * 4},
+        "gpu_launches": args.steps * (HOUFR * 6 + 1 + 2 * 5),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": None, "kernel": "k_sweep", "peak_kind": how,
+                     "alg_bytes_per_launch": alg_bytes, "launch_ms": sweep_ms, "launches": nsw.value},
+        "kernel_ms": {"sweep": sw_ms.value, "pt": pt_ms.value, "cluster": cl_ms.value, "step_total": ms},
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu:
+        su, dt = cpu_sample(os.cpu_count() or 1, sweeps=20)
+        line["cpu_baseline"] = {"value": su / dt / 1e12, "unit": "spin-updates/ps", "cores": os.cpu_count(),
+                                "kind": "port", "sample": "1 sample x 1 Metropolis sweep of the same geometry"}
+    print(json.dumps(line), flush=True)
+    job.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl" if args.impl == "ours" else "gloo")
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,721 @@
+// api.cu -- the C ABI of libeagb.so (declared in include/eagb.h).
+//
+// A context is one job: it owns every device buffer and one stream, and
+// enqueues the kernels of kernels.cu in the order of the reference driver
+// (PROGRAM/src/main.cu:142-230).  No call synchronises the device except the
+// ones that return data to the host.
+#include <curand.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "eagb.h"
+#include "host.hpp"
+#include "kernels.cuh"
+
+using namespace eagb;
+
+namespace {
+thread_local std::string g_err;
+
+int fail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CU(call)                                                                                  \
+  do {                                                                                            \
+    cudaError_t e_ = (call);                                                                      \
+    if (e_ != cudaSuccess) return fail(EA_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_));     \
+  } while (0)
+
+#define CR(call)                                                                                  \
+  do {                                                                                            \
+    curandStatus_t e_ = (call);                                                                   \
+    if (e_ != CURAND_STATUS_SUCCESS) return fail(EA_ERR_CURAND, "%s: curand status %d", #call, (int)e_); \
+  } while (0)
+
+template <class T>
+cudaError_t dalloc(T *&p, size_t n) {
+  return cudaMalloc((void **)&p, sizeof(T) * (n ? n : 1));
+}
+}  // namespace
+
+struct ea_ctx {
+  Geometry g;
+  int device = 0;
+  cudaStream_t st = nullptr;
+  JobDev j{};
+  std::vector<void *> owned;
+  bool have_temps = false;
+  bool energies_fresh = false;
+  // Houdayer
+  curandGenerator_t gen = nullptr;
+  uint64_t cuda_rng_offset = 0, seed_cluster = 0;
+  int nclust_cap = 0;
+  double *U = nullptr;
+  uint32_t *label = nullptr;
+  unsigned long long *Q = nullptr;
+  // measurement buffers
+  double *avgE = nullptr;
+  uint8_t *hist = nullptr;
+  int hist_cap = 0;
+  std::vector<int32_t> expoff;
+  double *exptab = nullptr;
+  // per-kernel timing (ea_profile)
+  bool prof_on = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_ev[EA_K_COUNT];
+  int64_t prof_n[EA_K_COUNT] = {};
+  double prof_ms[EA_K_COUNT] = {};
+};
+
+namespace {
+
+template <class T>
+int own(ea_ctx *c, T *&p, size_t n) {
+  cudaError_t e = dalloc(p, n);
+  if (e != cudaSuccess) return fail(EA_ERR_NOMEM, "cudaMalloc(%zu bytes): %s", sizeof(T) * n, cudaGetErrorString(e));
+  c->owned.push_back((void *)p);
+  cudaMemsetAsync(p, 0, sizeof(T) * (n ? n : 1), c->st);
+  return EA_OK;
+}
+
+int choose_kt(const Geometry &g) {
+  const char *env = getenv("EAGB_KT");
+  auto smem = [&](int kt) { return (size_t)g.NB * 2560 + (size_t)3 * g.NB * kt * g.NR * 8 + (size_t)kt * 32; };
+  const int cands_nr8[3] = {4, 2, 1}, cands_nr4[3] = {8, 4, 2}, cands_nr2[3] = {16, 8, 4};
+  const int *c = g.NR == 8 ? cands_nr8 : g.NR == 4 ? cands_nr4 : cands_nr2;
+  if (env) {
+    int kt = atoi(env);
+    for (int i = 0; i < 3; ++i)
+      if (c[i] == kt && smem(kt) <= 227 * 1024) return kt;
+  }
+  for (int i = 0; i < 3; ++i) {
+    const int kt = c[i];
+    const int tiles = (g.half + kt - 1) / kt;
+    if (smem(kt) <= 227 * 1024 && tiles >= 2 * 152) return kt;
+  }
+  for (int i = 2; i >= 0; --i)
+    if (smem(c[i]) <= 227 * 1024) return c[i];
+  return 0;
+}
+
+int check(ea_ctx *c) {
+  if (!c) return fail(EA_ERR_ARG, "null context");
+  return EA_OK;
+}
+
+int set_device(ea_ctx *c) {
+  CU(cudaSetDevice(c->device));
+  return EA_OK;
+}
+
+}  // namespace
+
+static void prof_collect(ea_ctx *c) {
+  for (int k = 0; k < EA_K_COUNT; ++k) {
+    for (auto &p : c->prof_ev[k]) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, p.first, p.second) == cudaSuccess) {
+        c->prof_ms[k] += ms;
+        c->prof_n[k] += 1;
+      }
+      cudaEventDestroy(p.first);
+      cudaEventDestroy(p.second);
+    }
+    c->prof_ev[k].clear();
+  }
+}
+
+
+extern "C" {
+
+const char *ea_last_error(void) { return g_err.c_str(); }
+int ea_version(void) { return EA_VERSION; }
+
+// ---------------------------------------------------------------------------
+// Host-side set-up
+// ---------------------------------------------------------------------------
+int ea_host_seeds(uint64_t master_J, uint64_t master_u, uint64_t master_MC, uint64_t master_cluster,
+                  const int32_t *list_samples, int32_t nsamples, int32_t nrep, uint64_t *seeds_J,
+                  uint64_t *seeds_u, uint64_t *seeds_MC) {
+  (void)master_cluster;
+  if (nsamples < 1 || nsamples > 32 || nrep < 1 || nrep > 64) return fail(EA_ERR_ARG, "bad sizes");
+  if (!master_J || !master_u || !master_MC) return fail(EA_ERR_ARG, "master seeds must be nonzero");
+  uint64_t tmp[64];
+  std::vector<int32_t> ls(nsamples);
+  for (int i = 0; i < nsamples; ++i) {
+    ls[i] = list_samples ? list_samples[i] : i;
+    if (ls[i] < 0 || ls[i] >= 32 || (i && ls[i] <= ls[i - 1])) return fail(EA_ERR_ARG, "sample list must be increasing in [0,32)");
+  }
+  // generate_seed_vectors (ini.c:32-59)
+  seeds_from_one(master_J, tmp, 32);
+  for (int i = 0; i < nsamples; ++i) seeds_J[i] = tmp[ls[i]];
+  seeds_from_one(master_u, tmp, 32);
+  for (int i = 0; i < nsamples; ++i) seeds_u[i] = tmp[ls[i]];
+  seeds_from_one(master_MC, tmp, nrep);
+  for (int r = 0; r < nrep; ++r) seeds_MC[r] = tmp[r];
+  return EA_OK;
+}
+
+int ea_host_generators(const uint64_t *seeds_MC, const int32_t *list_samples, int32_t nsamples, int32_t nrep,
+                       uint64_t seed_cluster, ea_generators *gen, ea_hq *pt_out) {
+  if (!seeds_MC || !gen || !pt_out || nrep < 1 || nrep > 64 || nsamples < 1 || nsamples > 32)
+    return fail(EA_ERR_ARG, "bad arguments");
+  if (!seed_cluster) return fail(EA_ERR_ARG, "cluster seed must be nonzero");
+  std::memset(gen, 0, sizeof(*gen));
+  // Init_Random (ini.c:61-101)
+  hq_seed(gen->rc, seed_cluster);
+  for (int r = 0; r < nrep; ++r) init_generators(seeds_MC[r], gen->prc[r], gen->xo[r], gen->keys[r]);
+  uint64_t tmp[32];
+  for (int r = 0; r < nrep; ++r) {
+    seeds_from_one(seeds_MC[r], tmp, 32);
+    for (int i = 0; i < nsamples; ++i) {
+      const int s = list_samples ? list_samples[i] : i;
+      // the reference passes this seed through an int (ini.c:63,90)
+      const int32_t s32 = (int32_t)(uint32_t)tmp[s];
+      hq_seed(pt_out[(size_t)i * nrep + r], (uint64_t)(int64_t)s32);
+    }
+  }
+  gen->cuda_rng_offset = 0;
+  gen->seed_cluster = seed_cluster;
+  return EA_OK;
+}
+
+int ea_host_init_spins(const ea_geom *gp, uint64_t seed_u, uint64_t *even, uint64_t *odd) {
+  Geometry g;
+  if (!gp || !g.set(*gp) || !even || !odd) return fail(EA_ERR_ARG, "bad geometry");
+  std::vector<uint8_t> uu;
+  init_spin_bytes(g, seed_u, uu);
+  for (int r = 0; r < g.NR; ++r)
+    for (int c = 0; c < g.NB; ++c) pack_clone(g, uu.data() + ((size_t)r * g.NB + c) * g.V, r, c, even, odd);
+  return EA_OK;
+}
+
+int ea_host_init_couplings(const ea_geom *gp, uint64_t seed_J, uint8_t *J6, uint64_t *Jw, int32_t *countJ) {
+  Geometry g;
+  if (!gp || !g.set(*gp) || !Jw) return fail(EA_ERR_ARG, "bad geometry");
+  std::vector<uint8_t> tmp;
+  if (!J6) { tmp.resize((size_t)6 * g.V); J6 = tmp.data(); }
+  const int cnt = init_couplings(g, seed_J, J6);
+  pack_couplings(g, J6, Jw);
+  if (countJ) *countJ = cnt;
+  return EA_OK;
+}
+
+int ea_host_unpack_replica(const ea_geom *gp, const uint64_t *even, const uint64_t *odd, int32_t rep, uint8_t *u) {
+  Geometry g;
+  if (!gp || !g.set(*gp) || rep < 0 || rep >= g.NR) return fail(EA_ERR_ARG, "bad arguments");
+  for (int c = 0; c < g.NB; ++c) unpack_clone(g, even, odd, rep, c, u + (size_t)c * g.V);
+  return EA_OK;
+}
+
+int ea_host_pack_replica(const ea_geom *gp, const uint8_t *u, int32_t rep, uint64_t *even, uint64_t *odd) {
+  Geometry g;
+  if (!gp || !g.set(*gp) || rep < 0 || rep >= g.NR) return fail(EA_ERR_ARG, "bad arguments");
+  for (int c = 0; c < g.NB; ++c) pack_clone(g, u + (size_t)c * g.V, rep, c, even, odd);
+  return EA_OK;
+}
+
+int ea_host_scalar_energy(const ea_geom *gp, const uint8_t *u, const uint8_t *J6, int32_t *E) {
+  Geometry g;
+  if (!gp || !g.set(*gp) || !u || !J6 || !E) return fail(EA_ERR_ARG, "bad arguments");
+  *E = scalar_energy(g, u, J6);
+  return EA_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Context
+// ---------------------------------------------------------------------------
+int ea_create(const ea_geom *gp, int32_t device, ea_ctx **out) {
+  if (!gp || !out) return fail(EA_ERR_ARG, "null argument");
+  ea_ctx *c = new ea_ctx();
+  if (!c->g.set(*gp)) { delete c; return fail(EA_ERR_ARG, "geometry: L, Lz multiples of 8, 2<=NB<=255, 1<=nsamples<=32"); }
+  const Geometry &g = c->g;
+  c->device = device;
+  int rc;
+  const int kt = choose_kt(g);
+  if (!kt || (g.NR != 8 && g.NR != 4 && g.NR != 2)) {
+    delete c;
+    return fail(EA_ERR_ARG, "unsupported NR=%d / NB=%d (thresholds of every temperature must fit in SMEM)", g.NR, g.NB);
+  }
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) { delete c; return fail(EA_ERR_CUDA, "cudaSetDevice(%d): %s", device, cudaGetErrorString(e)); }
+  e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { delete c; return fail(EA_ERR_CUDA, "stream: %s", cudaGetErrorString(e)); }
+  JobDev &j = c->j;
+  j.NB = g.NB; j.NR = g.NR; j.ns = g.ns; j.half = g.half; j.msc_l = g.msc_l; j.msc_s = g.msc_s;
+  j.msc_lz = g.msc_lz; j.L = g.L; j.Lz = g.Lz; j.V = g.V; j.bc = g.bc; j.kt = kt;
+  j.ntiles = (g.half + kt - 1) / kt;
+  const size_t nsr = (size_t)g.ns * g.NR;
+#define OWN(p, n) if ((rc = own(c, p, n)) != EA_OK) { ea_destroy(c); return rc; }
+  OWN(j.spins, g.ns * g.words_per_sample());
+  { unsigned long long *p; OWN(p, (size_t)g.ns * 12 * g.half); j.J = p; }
+  { int32_t *p; OWN(p, (size_t)12 * g.half); j.nbidx = p; }
+  { uint8_t *p; OWN(p, (size_t)2 * g.half); j.nbflag = p; }
+  { unsigned long long *p; OWN(p, (size_t)g.NB * 256); j.cum = p; }
+  { uint16_t *p; OWN(p, (size_t)g.NB * 256); j.pre = p; }
+  OWN(j.wctb, nsr * g.NB);
+  OWN(j.wbtc, nsr * g.NB);
+  OWN(j.ctr, (size_t)g.NR);
+  { uint32_t *p; OWN(p, (size_t)g.NR); j.keys = p; }
+  OWN(j.prc, (size_t)g.NR);
+  OWN(j.xo, (size_t)g.NR);
+  OWN(j.iter, 1);
+  OWN(j.epart, (size_t)j.ntiles * nsr * g.NB);
+  OWN(j.E, nsr * g.NB);
+  OWN(j.pt, nsr);
+  { double *p; OWN(p, (size_t)g.NB); j.betas = p; }
+  { int32_t *p; OWN(p, (size_t)g.NB); j.expoff = p; }
+  OWN(j.acc, nsr * (g.NB - 1));
+  OWN(j.att, nsr * (g.NB - 1));
+  OWN(j.accraw, nsr * (g.NB - 1));
+  OWN(j.inexact, 1);
+  OWN(j.rc, 1);
+  OWN(j.pairs, 4);
+  OWN(c->avgE, nsr * g.NB);
+  j.avgE = c->avgE;
+#undef OWN
+  std::vector<int32_t> idx;
+  std::vector<uint8_t> fl;
+  neighbour_tables(g, idx, fl);
+  CU(cudaMemcpyAsync((void *)j.nbidx, idx.data(), idx.size() * 4, cudaMemcpyHostToDevice, c->st));
+  CU(cudaMemcpyAsync((void *)j.nbflag, fl.data(), fl.size(), cudaMemcpyHostToDevice, c->st));
+  if ((rc = ea_set_permutations(c, nullptr)) != EA_OK) { ea_destroy(c); return rc; }
+  CU(cudaStreamSynchronize(c->st));
+  *out = c;
+  return EA_OK;
+}
+
+int ea_destroy(ea_ctx *c) {
+  if (!c) return EA_OK;
+  cudaSetDevice(c->device);
+  if (c->st) cudaStreamSynchronize(c->st);
+  if (c->gen) curandDestroyGenerator(c->gen);
+  prof_collect(c);
+  for (void *p : c->owned) cudaFree(p);
+  if (c->U) cudaFree(c->U);
+  if (c->label) cudaFree(c->label);
+  if (c->Q) cudaFree(c->Q);
+  if (c->hist) cudaFree(c->hist);
+  if (c->exptab) cudaFree(c->exptab);
+  if (c->st) cudaStreamDestroy(c->st);
+  delete c;
+  return EA_OK;
+}
+
+int ea_get_geom(const ea_ctx *c, ea_geom *g) {
+  if (!c || !g) return fail(EA_ERR_ARG, "null argument");
+  g->L = c->g.L; g->Lz = c->g.Lz; g->nbetas = c->g.NB; g->nrep = c->g.NR; g->nsamples = c->g.ns; g->bc = c->g.bc;
+  return EA_OK;
+}
+
+int ea_sync(ea_ctx *c) {
+  if (check(c)) return EA_ERR_ARG;
+  CU(cudaStreamSynchronize(c->st));
+  return EA_OK;
+}
+
+int ea_get_stream(ea_ctx *c, void **stream) {
+  if (check(c) || !stream) return fail(EA_ERR_ARG, "null argument");
+  *stream = (void *)c->st;
+  return EA_OK;
+}
+
+int ea_set_temperatures(ea_ctx *c, const double *betas, const uint64_t *cum) {
+  if (check(c) || !betas || !cum) return fail(EA_ERR_ARG, "null argument");
+  const Geometry &g = c->g;
+  for (int i = 0; i + 1 < g.NB; ++i)
+    if (betas[i] < betas[i + 1]) return fail(EA_ERR_ARG, "betas must be sorted from largest to smallest");
+  std::vector<uint16_t> pre((size_t)g.NB * 256);
+  for (int b = 0; b < g.NB; ++b) {
+    if (cum[(size_t)b * 256 + 255] != ~0ULL) return fail(EA_ERR_ARG, "threshold 255 of beta %d is not 2^64-1", b);
+    for (int n = 1; n < 256; ++n)
+      if (cum[(size_t)b * 256 + n] < cum[(size_t)b * 256 + n - 1]) return fail(EA_ERR_ARG, "thresholds of beta %d decrease", b);
+    presearch8(cum + (size_t)b * 256, pre.data() + (size_t)b * 256);
+  }
+  std::vector<double> tab;
+  pt_exp_table(betas, g.NB, tab, c->expoff);
+  if (set_device(c)) return EA_ERR_CUDA;
+  CU(cudaMemcpyAsync((void *)c->j.cum, cum, sizeof(uint64_t) * 256 * g.NB, cudaMemcpyHostToDevice, c->st));
+  CU(cudaMemcpyAsync((void *)c->j.pre, pre.data(), pre.size() * 2, cudaMemcpyHostToDevice, c->st));
+  CU(cudaMemcpyAsync((void *)c->j.betas, betas, sizeof(double) * g.NB, cudaMemcpyHostToDevice, c->st));
+  CU(cudaMemcpyAsync((void *)c->j.expoff, c->expoff.data(), sizeof(int32_t) * g.NB, cudaMemcpyHostToDevice, c->st));
+  CU(cudaStreamSynchronize(c->st));
+  if (c->exptab) cudaFree(c->exptab);
+  c->exptab = nullptr;
+  CU(dalloc(c->exptab, tab.size()));
+  CU(cudaMemcpy(c->exptab, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice));
+  c->j.exptab = c->exptab;
+  c->have_temps = true;
+  return EA_OK;
+}
+
+int ea_set_spins(ea_ctx *c, int32_t s, const uint64_t *even, const uint64_t *odd) {
+  if (check(c) || s < 0 || s >= c->g.ns || !even || !odd) return fail(EA_ERR_ARG, "bad arguments");
+  const size_t n = c->g.words_per_parity();
+  if (set_device(c)) return EA_ERR_CUDA;
+  unsigned long long *base = c->j.spins + (size_t)s * 2 * n;
+  CU(cudaMemcpyAsync(base, even, n * 8, cudaMemcpyHostToDevice, c->st));
+  CU(cudaMemcpyAsync(base + n, odd, n * 8, cudaMemcpyHostToDevice, c->st));
+  CU(cudaStreamSynchronize(c->st));
+  c->energies_fresh = false;
+  return EA_OK;
+}
+
+int ea_get_spins(ea_ctx *c, int32_t s, uint64_t *even, uint64_t *odd) {
+  if (check(c) || s < 0 || s >= c->g.ns || !even || !odd) return fail(EA_ERR_ARG, "bad arguments");
+  const size_t n = c->g.words_per_parity();
+  if (set_device(c)) return EA_ERR_CUDA;
+  const unsigned long long *base = c->j.spins + (size_t)s * 2 * n;
+  CU(cudaMemcpyAsync(even, base, n * 8, cudaMemcpyDeviceToHost, c->st));
+  CU(cudaMemcpyAsync(odd, base + n, n * 8, cudaMemcpyDeviceToHost, c->st));
+  CU(cudaStreamSynchronize(c->st));
+  return EA_OK;
+}
+
+int ea_set_couplings(ea_ctx *c, int32_t s, const uint64_t *Jw) {
+  if (check(c) || s < 0 || s >= c->g.ns || !Jw) return fail(EA_ERR_ARG, "bad arguments");
+  if (set_device(c)) return EA_ERR_CUDA;
+  const size_t n = (size_t)12 * c->g.half;
+  CU(cudaMemcpyAsync((void *)(c->j.J + (size_t)s * n), Jw, n * 8, cudaMemcpyHostToDevice, c->st));
+  CU(cudaStreamSynchronize(c->st));
+  return EA_OK;
+}
+
+int ea_set_generators(ea_ctx *c, const ea_generators *gen, const ea_hq *pt) {
+  if (check(c) || !gen || !pt) return fail(EA_ERR_ARG, "null argument");
+  const Geometry &g = c->g;
+  if (set_device(c)) return EA_ERR_CUDA;
+  CU(cudaMemcpyAsync(c->j.prc, gen->prc, sizeof(ea_hq) * g.NR, cudaMemcpyHostToDevice, c->st));
+  CU(cudaMemcpyAsync(c->j.xo, gen->xo, sizeof(ea_xoshiro) * g.NR, cudaMemcpyHostToDevice, c->st));
+  CU(cudaMemcpyAsync((void *)c->j.keys, gen->keys, sizeof(uint32_t) * g.NR, cudaMemcpyHostToDevice, c->st));
+  CU(cudaMemcpyAsync(c->j.rc, &gen->rc, sizeof(ea_hq), cudaMemcpyHostToDevice, c->st));
+  CU(cudaMemcpyAsync(c->j.pt, pt, sizeof(ea_hq) * g.ns * g.NR, cudaMemcpyHostToDevice, c->st));
+  CU(cudaStreamSynchronize(c->st));
+  if (c->gen && (gen->seed_cluster != c->seed_cluster || gen->cuda_rng_offset != c->cuda_rng_offset)) {
+    curandDestroyGenerator(c->gen);
+    c->gen = nullptr;
+  }
+  c->cuda_rng_offset = gen->cuda_rng_offset;
+  c->seed_cluster = gen->seed_cluster;
+  return EA_OK;
+}
+
+int ea_get_generators(ea_ctx *c, ea_generators *gen, ea_hq *pt) {
+  if (check(c) || !gen) return fail(EA_ERR_ARG, "null argument");
+  const Geometry &g = c->g;
+  if (set_device(c)) return EA_ERR_CUDA;
+  std::memset(gen, 0, sizeof(*gen));
+  CU(cudaMemcpyAsync(gen->prc, c->j.prc, sizeof(ea_hq) * g.NR, cudaMemcpyDeviceToHost, c->st));
+  CU(cudaMemcpyAsync(gen->xo, c->j.xo, sizeof(ea_xoshiro) * g.NR, cudaMemcpyDeviceToHost, c->st));
+  CU(cudaMemcpyAsync(gen->keys, c->j.keys, sizeof(uint32_t) * g.NR, cudaMemcpyDeviceToHost, c->st));
+  CU(cudaMemcpyAsync(&gen->rc, c->j.rc, sizeof(ea_hq), cudaMemcpyDeviceToHost, c->st));
+  if (pt) CU(cudaMemcpyAsync(pt, c->j.pt, sizeof(ea_hq) * g.ns * g.NR, cudaMemcpyDeviceToHost, c->st));
+  CU(cudaStreamSynchronize(c->st));
+  gen->cuda_rng_offset = c->cuda_rng_offset;
+  gen->seed_cluster = c->seed_cluster;
+  return EA_OK;
+}
+
+int ea_set_permutations(ea_ctx *c, const uint8_t *wctb) {
+  if (check(c)) return EA_ERR_ARG;
+  const Geometry &g = c->g;
+  const size_t n = (size_t)g.ns * g.NR * g.NB;
+  std::vector<uint8_t> a(n), b(n);
+  for (size_t o = 0; o < (size_t)g.ns * g.NR; ++o) {
+    std::vector<int> seen(g.NB, 0);
+    for (int i = 0; i < g.NB; ++i) {
+      const uint8_t v = wctb ? wctb[o * g.NB + i] : (uint8_t)i;
+      if (v >= g.NB || seen[v]++) return fail(EA_ERR_ARG, "which_clon_this_beta is not a permutation");
+      a[o * g.NB + i] = v;
+      b[o * g.NB + v] = (uint8_t)i;
+    }
+  }
+  if (set_device(c)) return EA_ERR_CUDA;
+  CU(cudaMemcpyAsync(c->j.wctb, a.data(), n, cudaMemcpyHostToDevice, c->st));
+  CU(cudaMemcpyAsync(c->j.wbtc, b.data(), n, cudaMemcpyHostToDevice, c->st));
+  CU(cudaStreamSynchronize(c->st));
+  return EA_OK;
+}
+
+int ea_get_permutations(ea_ctx *c, uint8_t *wctb, uint8_t *wbtc) {
+  if (check(c)) return EA_ERR_ARG;
+  const size_t n = (size_t)c->g.ns * c->g.NR * c->g.NB;
+  if (set_device(c)) return EA_ERR_CUDA;
+  if (wctb) CU(cudaMemcpyAsync(wctb, c->j.wctb, n, cudaMemcpyDeviceToHost, c->st));
+  if (wbtc) CU(cudaMemcpyAsync(wbtc, c->j.wbtc, n, cudaMemcpyDeviceToHost, c->st));
+  CU(cudaStreamSynchronize(c->st));
+  return EA_OK;
+}
+
+int ea_get_pt_stats(ea_ctx *c, double *acc, double *att, double *accraw) {
+  if (check(c)) return EA_ERR_ARG;
+  const size_t n = (size_t)c->g.ns * c->g.NR * (c->g.NB - 1);
+  if (set_device(c)) return EA_ERR_CUDA;
+  if (acc) CU(cudaMemcpyAsync(acc, c->j.acc, n * 8, cudaMemcpyDeviceToHost, c->st));
+  if (att) CU(cudaMemcpyAsync(att, c->j.att, n * 8, cudaMemcpyDeviceToHost, c->st));
+  if (accraw) CU(cudaMemcpyAsync(accraw, c->j.accraw, n * 8, cudaMemcpyDeviceToHost, c->st));
+  CU(cudaStreamSynchronize(c->st));
+  return EA_OK;
+}
+
+int ea_reset_pt_stats(ea_ctx *c) {
+  if (check(c)) return EA_ERR_ARG;
+  const size_t n = (size_t)c->g.ns * c->g.NR * (c->g.NB - 1);
+  if (set_device(c)) return EA_ERR_CUDA;
+  CU(cudaMemsetAsync(c->j.acc, 0, n * 8, c->st));
+  CU(cudaMemsetAsync(c->j.att, 0, n * 8, c->st));
+  CU(cudaMemsetAsync(c->j.accraw, 0, n * 8, c->st));
+  return EA_OK;
+}
+
+int ea_set_counter(ea_ctx *c, int64_t iter, uint32_t jobid) {
+  if (check(c) || iter < 0 || jobid >= (1u << 14)) return fail(EA_ERR_ARG, "iter >= 0 and job id < 2^14");
+  if (set_device(c)) return EA_ERR_CUDA;
+  long long v = iter;
+  CU(cudaMemcpyAsync(c->j.iter, &v, 8, cudaMemcpyHostToDevice, c->st));
+  CU(cudaStreamSynchronize(c->st));
+  c->j.jobid = jobid;
+  return EA_OK;
+}
+
+int ea_get_counter(ea_ctx *c, int64_t *iter) {
+  if (check(c) || !iter) return EA_ERR_ARG;
+  if (set_device(c)) return EA_ERR_CUDA;
+  long long v = 0;
+  CU(cudaMemcpyAsync(&v, c->j.iter, 8, cudaMemcpyDeviceToHost, c->st));
+  CU(cudaStreamSynchronize(c->st));
+  *iter = v;
+  return EA_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Hot path
+// ---------------------------------------------------------------------------
+// Event pair around one launch when profiling is on (ea_profile).
+static cudaEvent_t prof_begin(ea_ctx *c) {
+  if (!c->prof_on) return nullptr;
+  cudaEvent_t e;
+  if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+  cudaEventRecord(e, c->st);
+  return e;
+}
+
+static void prof_end(ea_ctx *c, int kind, cudaEvent_t b) {
+  if (!b) return;
+  cudaEvent_t e;
+  if (cudaEventCreate(&e) != cudaSuccess) return;
+  cudaEventRecord(e, c->st);
+  c->prof_ev[kind].push_back({b, e});
+}
+
+static int mc(ea_ctx *c, int n) {
+  for (int sw = 0; sw < n; ++sw)
+    for (int p = 0; p < 2; ++p) {
+      CU(launch_fill_bits(c->j, p, c->st));
+      cudaEvent_t b = prof_begin(c);
+      CU(launch_sweep(c->j, p, sw == n - 1 && p == 1, c->st));
+      prof_end(c, EA_K_SWEEP, b);
+    }
+  if (n > 0) {
+    CU(launch_energy_reduce(c->j, c->st));
+    c->energies_fresh = true;
+  }
+  return EA_OK;
+}
+
+int ea_monte_carlo(ea_ctx *c, int32_t nsweeps) {
+  if (check(c) || nsweeps < 0) return fail(EA_ERR_ARG, "bad arguments");
+  if (!c->have_temps) return fail(EA_ERR_STATE, "temperatures not set");
+  if (set_device(c)) return EA_ERR_CUDA;
+  return mc(c, nsweeps);
+}
+
+static int measure(ea_ctx *c) {
+  cudaEvent_t b = prof_begin(c);
+  CU(launch_energy(c->j, c->st));
+  CU(launch_energy_reduce(c->j, c->st));
+  prof_end(c, EA_K_ENERGY, b);
+  c->energies_fresh = true;
+  return EA_OK;
+}
+
+int ea_measure_energy(ea_ctx *c, int32_t *out) {
+  if (check(c)) return EA_ERR_ARG;
+  if (set_device(c)) return EA_ERR_CUDA;
+  int rc = measure(c);
+  if (rc) return rc;
+  if (out) {
+    CU(cudaMemcpyAsync(out, c->j.E, sizeof(int32_t) * c->g.ns * c->g.NR * c->g.NB, cudaMemcpyDeviceToHost, c->st));
+    CU(cudaStreamSynchronize(c->st));
+  }
+  return EA_OK;
+}
+
+static int pt(ea_ctx *c) {
+  cudaEvent_t b = prof_begin(c);
+  CU(launch_pt(c->j, c->st));
+  prof_end(c, EA_K_PT, b);
+  return EA_OK;
+}
+
+int ea_parallel_tempering(ea_ctx *c) {
+  if (check(c)) return EA_ERR_ARG;
+  if (!c->have_temps) return fail(EA_ERR_STATE, "temperatures not set");
+  if (!c->energies_fresh) return fail(EA_ERR_STATE, "no energies of the current state (run ea_monte_carlo or ea_measure_energy)");
+  if (set_device(c)) return EA_ERR_CUDA;
+  return pt(c);
+}
+
+static int ensure_cluster(ea_ctx *c, int nclust) {
+  const Geometry &g = c->g;
+  if (!c->U) {
+    CU(dalloc(c->U, (size_t)g.V * g.NB * g.ns));
+    c->j.U = c->U;
+  }
+  if (nclust > c->nclust_cap) {
+    if (c->label) cudaFree(c->label);
+    if (c->Q) cudaFree(c->Q);
+    c->label = nullptr; c->Q = nullptr;
+    CU(dalloc(c->label, (size_t)g.V * nclust * g.ns));
+    CU(dalloc(c->Q, (size_t)2 * g.half * nclust * g.ns));
+    c->nclust_cap = nclust;
+  }
+  c->j.label = c->label;
+  c->j.Q = c->Q;
+  c->j.nclust = nclust;
+  if (!c->gen) {
+    // ClusterInit (HoudayerXEA.cu:174-178): default pseudo generator (XORWOW),
+    // seed_Cluster, and the offset already consumed.
+    CR(curandCreateGenerator(&c->gen, CURAND_RNG_PSEUDO_DEFAULT));
+    CR(curandSetPseudoRandomGeneratorSeed(c->gen, (unsigned long long)c->seed_cluster));
+    if (c->cuda_rng_offset > 0) CR(curandSetGeneratorOffset(c->gen, c->cuda_rng_offset));
+    CR(curandSetStream(c->gen, c->st));
+  }
+  return EA_OK;
+}
+
+static int houdayer(ea_ctx *c, int nclust) {
+  const Geometry &g = c->g;
+  if (g.NR < 4) return fail(EA_ERR_ARG, "the Houdayer move needs at least 2 replicas per group");
+  if (nclust <= 0) nclust = (int)std::lround(g.NB * 0.5);
+  if (nclust > g.NB) nclust = g.NB;
+  int rc = ensure_cluster(c, nclust);
+  if (rc) return rc;
+  CU(launch_houdayer_pairs(c->j, c->st));
+  const size_t tot = (size_t)g.V * g.NB * g.ns;
+  for (int grp = 0; grp < 2; ++grp) {
+    // ClusterStep (HoudayerXEA.cu:189-195): V*NB*nsamples uniforms per group
+    CR(curandGenerateUniformDouble(c->gen, c->U, tot));
+    c->cuda_rng_offset += tot;
+    cudaEvent_t b = prof_begin(c);
+    CU(launch_houdayer_group(c->j, grp, c->st));
+    prof_end(c, EA_K_CLUSTER, b);
+  }
+  c->energies_fresh = false;
+  return EA_OK;
+}
+
+int ea_houdayer(ea_ctx *c, int32_t nclust) {
+  if (check(c)) return EA_ERR_ARG;
+  if (set_device(c)) return EA_ERR_CUDA;
+  return houdayer(c, nclust);
+}
+
+static void trw(int itmax, int *frec, int *maxit) {
+  for (int f = 1; f <= itmax; ++f)
+    if (itmax % f == 0 && itmax / f <= 512) { *frec = f; *maxit = itmax / f; return; }
+  *frec = 1; *maxit = itmax;
+}
+
+int ea_run_bin(ea_ctx *c, const ea_cadence *cad, double *avgE, uint8_t *hist, int32_t *maxit_trw) {
+  if (check(c) || !cad || cad->itmax < 1 || cad->houfr < 1 || cad->mesfr < 1 || cad->ptfr < 0)
+    return fail(EA_ERR_ARG, "bad cadence");
+  if (!c->have_temps) return fail(EA_ERR_STATE, "temperatures not set");
+  if (set_device(c)) return EA_ERR_CUDA;
+  const Geometry &g = c->g;
+  int frec, maxit;
+  trw(cad->itmax, &frec, &maxit);
+  const size_t nsr = (size_t)g.ns * g.NR;
+  if (maxit > c->hist_cap) {
+    if (c->hist) cudaFree(c->hist);
+    c->hist = nullptr;
+    CU(dalloc(c->hist, nsr * maxit * g.NB));
+    c->hist_cap = maxit;
+  }
+  c->j.hist = c->hist;
+  c->j.maxit_trw = maxit;
+  CU(cudaMemsetAsync(c->avgE, 0, nsr * g.NB * 8, c->st));
+  CU(cudaMemsetAsync(c->hist, 0, nsr * maxit * g.NB, c->st));
+  int rc;
+  for (int it = 0; it < cad->itmax; ++it) {
+    for (int im = 0; im < cad->mesfr; ++im) {
+      for (int ih = 0; ih < cad->houfr; ++ih) {
+        if ((rc = mc(c, cad->ptfr))) return rc;
+        if (!c->energies_fresh && (rc = measure(c))) return rc;
+        if ((rc = pt(c))) return rc;
+      }
+      if (cad->cluster && (rc = houdayer(c, cad->nclust))) return rc;
+    }
+    if ((rc = measure(c))) return rc;
+    CU(launch_measure(c->j, (it % frec == frec - 1) ? it / frec : -1, c->st));
+  }
+  if (avgE) CU(cudaMemcpyAsync(avgE, c->avgE, nsr * g.NB * 8, cudaMemcpyDeviceToHost, c->st));
+  if (hist) CU(cudaMemcpyAsync(hist, c->hist, nsr * maxit * g.NB, cudaMemcpyDeviceToHost, c->st));
+  CU(cudaStreamSynchronize(c->st));
+  if (maxit_trw) *maxit_trw = maxit;
+  unsigned long long inex = 0;
+  CU(cudaMemcpy(&inex, c->j.inexact, 8, cudaMemcpyDeviceToHost));
+  if (inex) return fail(EA_ERR_INEXACT, "%llu tempering decisions fell outside the exact exp table", inex);
+  return EA_OK;
+}
+
+int ea_profile(ea_ctx *c, int32_t on) {
+  if (check(c)) return EA_ERR_ARG;
+  if (set_device(c)) return EA_ERR_CUDA;
+  CU(cudaStreamSynchronize(c->st));
+  prof_collect(c);
+  for (int k = 0; k < EA_K_COUNT; ++k) { c->prof_n[k] = 0; c->prof_ms[k] = 0; }
+  c->prof_on = on != 0;
+  return EA_OK;
+}
+
+int ea_kernel_time(ea_ctx *c, int32_t kind, int64_t *launches, double *total_ms) {
+  if (check(c) || kind < 0 || kind >= EA_K_COUNT) return fail(EA_ERR_ARG, "bad kernel kind");
+  if (set_device(c)) return EA_ERR_CUDA;
+  CU(cudaStreamSynchronize(c->st));
+  prof_collect(c);
+  if (launches) *launches = c->prof_n[kind];
+  if (total_ms) *total_ms = c->prof_ms[kind];
+  return EA_OK;
+}
+
+int ea_curand_uniforms(int32_t device, uint64_t seed, uint64_t offset, uint64_t n, double *out) {
+  if (!out) return fail(EA_ERR_ARG, "null output");
+  CU(cudaSetDevice(device));
+  double *d = nullptr;
+  CU(dalloc(d, n));
+  curandGenerator_t gen;
+  curandStatus_t s = curandCreateGenerator(&gen, CURAND_RNG_PSEUDO_DEFAULT);
+  if (s == CURAND_STATUS_SUCCESS) s = curandSetPseudoRandomGeneratorSeed(gen, seed);
+  if (s == CURAND_STATUS_SUCCESS && offset) s = curandSetGeneratorOffset(gen, offset);
+  if (s == CURAND_STATUS_SUCCESS) s = curandGenerateUniformDouble(gen, d, n);
+  curandDestroyGenerator(gen);
+  if (s != CURAND_STATUS_SUCCESS) { cudaFree(d); return fail(EA_ERR_CURAND, "curand status %d", (int)s); }
+  cudaError_t e = cudaMemcpy(out, d, n * 8, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return fail(EA_ERR_CUDA, "%s", cudaGetErrorString(e));
+  return EA_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,62 @@
+// kernels.cuh -- device-side job descriptor and kernel launchers.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "eagb.h"
+
+namespace eagb {
+
+// Everything a kernel needs about one job, by value (kernel parameter).
+// All arrays live in device memory, in the reference's layouts.
+struct JobDev {
+  int NB, NR, ns, half, msc_l, msc_s, msc_lz, L, Lz, V, bc;
+  unsigned long long *spins;        // [s][parity][clone][half][rep]
+  const unsigned long long *J;      // [s][parity][dir][half]
+  const int32_t *nbidx;             // [parity][dir][half]
+  const uint8_t *nbflag;            // [parity][half]
+  const unsigned long long *cum;    // [NB][256] thresholds
+  const uint16_t *pre;              // [NB][256] 8-bit pre-search
+  uint8_t *wctb, *wbtc;             // [s][rep][NB]
+  uint4 *ctr;                       // [NR] Philox counters of the current half-sweep
+  const uint32_t *keys;             // [NR]
+  ea_hq *prc;                       // [NR]
+  ea_xoshiro *xo;                   // [NR]
+  long long *iter;                  // half-sweep counter (device scalar)
+  uint32_t jobid;
+  int32_t *epart;                   // [ntiles][s][clone][rep] energy partial sums
+  int ntiles, kt;
+  int32_t *E;                       // [s][rep][clone]
+  // parallel tempering
+  ea_hq *pt;                        // [s][rep]
+  const double *betas;              // [NB]
+  const double *exptab;             // glibc exp table
+  const int32_t *expoff;            // [NB]
+  double *acc, *att, *accraw;       // [s][rep][NB-1]
+  unsigned long long *inexact;      // decisions decided outside the table (u == 0)
+  // measurements
+  double *avgE;                     // [s][rep][NB]
+  uint8_t *hist;                    // [s][rep][maxit][NB]
+  int maxit_trw;
+  // Houdayer
+  ea_hq *rc;
+  int32_t *pairs;                   // [2 groups][2]
+  unsigned long long *Q;            // [s][nclust][2][half] overlap words
+  uint32_t *label;                  // [s][nclust][V]
+  const double *U;                  // [s][NB][V] uniforms of the current group
+  int nclust;
+};
+
+// Tile width (half-sites per CTA) of the fused sweep kernel.
+int sweep_kt(const JobDev &j);
+size_t sweep_smem_bytes(const JobDev &j);
+
+cudaError_t launch_fill_bits(const JobDev &j, int parity, cudaStream_t st);
+cudaError_t launch_sweep(const JobDev &j, int parity, bool energy, cudaStream_t st);
+cudaError_t launch_energy(const JobDev &j, cudaStream_t st);
+cudaError_t launch_energy_reduce(const JobDev &j, cudaStream_t st);
+cudaError_t launch_pt(const JobDev &j, cudaStream_t st);
+cudaError_t launch_measure(const JobDev &j, int itm, cudaStream_t st);
+cudaError_t launch_houdayer_pairs(const JobDev &j, cudaStream_t st);
+cudaError_t launch_houdayer_group(const JobDev &j, int group, cudaStream_t st);
+
+}  // namespace eagb

@@ -1,0 +1,252 @@
+"""ctypes binding of libeagb.so (include/eagb.h) for tests, bench and scripts.
+
+The library is the product; this module only marshals numpy arrays through
+the C ABI.  It refuses to run without the compiled library: there is no
+Python or CPU implementation of the hot path behind it.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libeagb.so")
+
+EA_PBC, EA_OBC, EA_OBC_WEAK, EA_OBC_STRONG = 0, 1, 2, 3
+BC = {"PBC": EA_PBC, "OBC": EA_OBC, "WEAK": EA_OBC_WEAK, "STRONG": EA_OBC_STRONG}
+
+
+class Geom(C.Structure):
+    _fields_ = [("L", C.c_int32), ("Lz", C.c_int32), ("nbetas", C.c_int32), ("nrep", C.c_int32),
+                ("nsamples", C.c_int32), ("bc", C.c_int32)]
+
+
+class HQ(C.Structure):
+    _fields_ = [("ira", C.c_uint64 * 256), ("PR", C.c_uint64), ("zseed", C.c_uint64), ("final", C.c_uint64),
+                ("ip", C.c_uint8), ("ip1", C.c_uint8), ("ip2", C.c_uint8), ("ip3", C.c_uint8),
+                ("padding", C.c_uint8 * 4)]
+
+
+class Xoshiro(C.Structure):
+    _fields_ = [("s", C.c_uint64 * 4), ("t", C.c_uint64), ("final", C.c_uint64)]
+
+
+class Generators(C.Structure):
+    _fields_ = [("prc", HQ * 64), ("xo", Xoshiro * 64), ("keys", C.c_uint32 * 64), ("rc", HQ),
+                ("cuda_rng_offset", C.c_uint64), ("seed_cluster", C.c_uint64)]
+
+
+class Cadence(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in ("itmax", "houfr", "mesfr", "ptfr", "cluster", "nclust")]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libeagb.so is not built (run python ea-lcd-mc_gb300/build.py)")
+        _lib = C.CDLL(LIB_PATH)
+        _lib.ea_last_error.restype = C.c_char_p
+    return _lib
+
+
+class EAError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("ea error %d: %s" % (code, msg))
+        self.code = code
+
+
+def _ck(rc):
+    if rc != 0:
+        raise EAError(rc, lib().ea_last_error().decode())
+
+
+def P(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def geom(L, Lz, NB, NR=8, nsamples=1, bc=EA_OBC):
+    return Geom(L, Lz, NB, NR, nsamples, bc)
+
+
+def sizes(g):
+    half = (g.L // 4) * (g.L // 4) * (g.Lz // 4) // 2
+    return half, g.L * g.L * g.Lz
+
+
+def host_seeds(masters, nsamples, nrep=8, list_samples=None):
+    sJ = np.zeros(nsamples, np.uint64)
+    su = np.zeros(nsamples, np.uint64)
+    sMC = np.zeros(nrep, np.uint64)
+    ls = None if list_samples is None else np.ascontiguousarray(list_samples, np.int32)
+    _ck(lib().ea_host_seeds(C.c_uint64(masters[0]), C.c_uint64(masters[1]), C.c_uint64(masters[2]),
+                            C.c_uint64(masters[3]), None if ls is None else P(ls), nsamples, nrep, P(sJ), P(su),
+                            P(sMC)))
+    return sJ, su, sMC
+
+
+def host_generators(seeds_MC, nsamples, seed_cluster, list_samples=None):
+    nrep = len(seeds_MC)
+    gen = Generators()
+    pt = (HQ * (nsamples * nrep))()
+    sMC = np.ascontiguousarray(seeds_MC, np.uint64)
+    ls = None if list_samples is None else np.ascontiguousarray(list_samples, np.int32)
+    _ck(lib().ea_host_generators(P(sMC), None if ls is None else P(ls), nsamples, nrep, C.c_uint64(seed_cluster),
+                                 C.byref(gen), pt))
+    return gen, pt
+
+
+def host_init_spins(g, seed_u):
+    half, V = sizes(g)
+    n = g.nbetas * half * g.nrep
+    ev = np.zeros(n, np.uint64)
+    od = np.zeros(n, np.uint64)
+    _ck(lib().ea_host_init_spins(C.byref(g), C.c_uint64(seed_u), P(ev), P(od)))
+    return ev, od
+
+
+def host_init_couplings(g, seed_J):
+    half, V = sizes(g)
+    J6 = np.zeros(6 * V, np.uint8)
+    Jw = np.zeros(12 * half, np.uint64)
+    cnt = C.c_int32(0)
+    _ck(lib().ea_host_init_couplings(C.byref(g), C.c_uint64(seed_J), P(J6), P(Jw), C.byref(cnt)))
+    return J6, Jw, cnt.value
+
+
+class Job:
+    """One simulation job on one GPU (an ea_ctx)."""
+
+    def __init__(self, g, device=0):
+        self.g = g
+        self.half, self.V = sizes(g)
+        self.ctx = C.c_void_p()
+        _ck(lib().ea_create(C.byref(g), device, C.byref(self.ctx)))
+
+    def close(self):
+        if self.ctx:
+            lib().ea_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # inputs / outputs
+    def set_temperatures(self, betas, cum):
+        b = np.ascontiguousarray(betas, np.float64)
+        c = np.ascontiguousarray(cum, np.uint64)
+        _ck(lib().ea_set_temperatures(self.ctx, P(b), P(c)))
+
+    def set_spins(self, s, even, odd):
+        _ck(lib().ea_set_spins(self.ctx, s, P(np.ascontiguousarray(even, np.uint64)),
+                               P(np.ascontiguousarray(odd, np.uint64))))
+
+    def get_spins(self, s):
+        n = self.g.nbetas * self.half * self.g.nrep
+        ev = np.zeros(n, np.uint64)
+        od = np.zeros(n, np.uint64)
+        _ck(lib().ea_get_spins(self.ctx, s, P(ev), P(od)))
+        return ev, od
+
+    def set_couplings(self, s, Jw):
+        _ck(lib().ea_set_couplings(self.ctx, s, P(np.ascontiguousarray(Jw, np.uint64))))
+
+    def set_generators(self, gen, pt):
+        _ck(lib().ea_set_generators(self.ctx, C.byref(gen), pt))
+
+    def get_generators(self):
+        gen = Generators()
+        pt = (HQ * (self.g.nsamples * self.g.nrep))()
+        _ck(lib().ea_get_generators(self.ctx, C.byref(gen), pt))
+        return gen, pt
+
+    def set_permutations(self, wctb=None):
+        if wctb is None:
+            _ck(lib().ea_set_permutations(self.ctx, None))
+        else:
+            _ck(lib().ea_set_permutations(self.ctx, P(np.ascontiguousarray(wctb, np.uint8))))
+
+    def get_permutations(self):
+        shape = (self.g.nsamples, self.g.nrep, self.g.nbetas)
+        a = np.zeros(shape, np.uint8)
+        b = np.zeros(shape, np.uint8)
+        _ck(lib().ea_get_permutations(self.ctx, P(a), P(b)))
+        return a, b
+
+    def get_pt_stats(self):
+        shape = (self.g.nsamples, self.g.nrep, self.g.nbetas - 1)
+        acc, att, raw = (np.zeros(shape) for _ in range(3))
+        _ck(lib().ea_get_pt_stats(self.ctx, P(acc), P(att), P(raw)))
+        return acc, att, raw
+
+    def set_counter(self, it, jobid=0):
+        _ck(lib().ea_set_counter(self.ctx, C.c_int64(it), C.c_uint32(jobid)))
+
+    def get_counter(self):
+        v = C.c_int64(0)
+        _ck(lib().ea_get_counter(self.ctx, C.byref(v)))
+        return v.value
+
+    # hot path
+    def monte_carlo(self, n):
+        _ck(lib().ea_monte_carlo(self.ctx, n))
+
+    def measure_energy(self):
+        E = np.zeros((self.g.nsamples, self.g.nrep, self.g.nbetas), np.int32)
+        _ck(lib().ea_measure_energy(self.ctx, P(E)))
+        return E
+
+    def parallel_tempering(self):
+        _ck(lib().ea_parallel_tempering(self.ctx))
+
+    def houdayer(self, nclust=0):
+        _ck(lib().ea_houdayer(self.ctx, nclust))
+
+    def run_bin(self, itmax, houfr, mesfr, ptfr, cluster=True, nclust=0):
+        cad = Cadence(itmax, houfr, mesfr, ptfr, int(cluster), nclust)
+        avg = np.zeros((self.g.nsamples, self.g.nrep, self.g.nbetas))
+        hist = np.zeros(self.g.nsamples * self.g.nrep * 512 * self.g.nbetas, np.uint8)
+        mx = C.c_int32(0)
+        _ck(lib().ea_run_bin(self.ctx, C.byref(cad), P(avg), P(hist), C.byref(mx)))
+        m = mx.value
+        return avg, hist[:self.g.nsamples * self.g.nrep * m * self.g.nbetas].reshape(
+            self.g.nsamples, self.g.nrep, m, self.g.nbetas)
+
+    def sync(self):
+        _ck(lib().ea_sync(self.ctx))
+
+    def stream(self):
+        v = C.c_void_p()
+        _ck(lib().ea_get_stream(self.ctx, C.byref(v)))
+        return v.value
+
+
+def curand_uniforms(seed, offset, n, device=0):
+    out = np.zeros(n, np.float64)
+    _ck(lib().ea_curand_uniforms(device, C.c_uint64(seed), C.c_uint64(offset), C.c_uint64(n), P(out)))
+    return out
+
+
+def new_job(L, Lz, betas, cum, nsamples=1, NR=8, bc=EA_OBC, masters=(1, 2, 3, 4), list_samples=None,
+            device=0, iter0=0, jobid=0):
+    """A job initialised exactly as the reference initialises a new run (flag 1)."""
+    g = geom(L, Lz, len(betas), NR, nsamples, bc)
+    job = Job(g, device)
+    job.set_temperatures(betas, cum)
+    sJ, su, sMC = host_seeds(masters, nsamples, NR, list_samples)
+    gen, pt = host_generators(sMC, nsamples, masters[3], list_samples)
+    job.set_generators(gen, pt)
+    for s in range(nsamples):
+        ev, od = host_init_spins(g, int(su[s]))
+        job.set_spins(s, ev, od)
+        J6, Jw, _ = host_init_couplings(g, int(sJ[s]))
+        job.set_couplings(s, Jw)
+    job.set_permutations(None)
+    job.set_counter(iter0, jobid)
+    return job

@@ -1,0 +1,174 @@
+/*
+ * eagb.h -- C ABI of the GB300-native EA-LCD-MC simulation library (libeagb.so).
+ *
+ * One context = one simulation job as the reference runs it in one process:
+ * `nsamples` disorder samples ("nbits" on the reference command line) of an
+ * L x L x Lz tube, NR replicas and NB temperatures, in the reference's
+ * multispin layout (64 spatial sub-blocks per 64-bit word).  The context owns
+ * all device memory and one CUDA stream; host buffers are caller-owned and
+ * only copied.  Every function returns EA_OK (0) or a negative EA_ERR_*
+ * code and never exits the process; ea_last_error() describes the last
+ * failure of the calling thread.  One context must not be used by two host
+ * threads at the same time.
+ *
+ * Layouts (identical to the reference's host arrays):
+ *   spins    even/odd arrays [clone][half][replica] uint64 (PROGRAM/src/ini.c:339-383)
+ *   couplings Jw[parity][dir][half] uint64, dir = +x,+y,+z,-x,-y,-z (ini.c:672-730)
+ *   permutations which_clon_this_beta[sample][replica][beta] (header.h:153-154)
+ *   energies [sample][replica][clone] int32, E = 3V - 2 * unsatisfied bonds (main.cu:1379)
+ *   thresholds cum[beta][256]: the 64-bit cumulative thresholds of the LUT
+ *             file, 'umbrales' (PROGRAM/input/create_LUT.c:301-326)
+ */
+#ifndef EAGB_H
+#define EAGB_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EA_VERSION 100
+
+enum {
+  EA_OK = 0,
+  EA_ERR_ARG = -1,     /* invalid argument or geometry */
+  EA_ERR_CUDA = -2,    /* CUDA runtime error */
+  EA_ERR_NOMEM = -3,   /* device or host allocation failed */
+  EA_ERR_STATE = -4,   /* call out of order (e.g. run before inputs are set) */
+  EA_ERR_CURAND = -5,  /* cuRAND error */
+  EA_ERR_IO = -6,      /* file I/O or format error */
+  EA_ERR_INEXACT = -7  /* a PT decision fell outside the exact glibc-exp table (never seen) */
+};
+
+/* Boundary conditions along z (PROGRAM/Makefile:8-30, ini.c:551-641). */
+enum { EA_PBC = 0, EA_OBC = 1, EA_OBC_WEAK = 2, EA_OBC_STRONG = 3 };
+
+typedef struct {
+  int32_t L, Lz;     /* multiples of 8 (header.h:41-47) */
+  int32_t nbetas;    /* NBETAS, 2..255 */
+  int32_t nrep;      /* NR, 8 in the reference (header.h:14); the Houdayer move needs NR/2 >= 2 */
+  int32_t nsamples;  /* nbits, 1..32 (main.cu:53) */
+  int32_t bc;        /* EA_PBC / EA_OBC / EA_OBC_WEAK / EA_OBC_STRONG */
+} ea_geom;
+
+/* Host generator states, byte-compatible with the reference's structs
+ * (PROGRAM/include/random_generator.h:31-46) and its checkpoint files. */
+typedef struct {
+  uint64_t ira[256];
+  uint64_t PR, zseed, final;
+  uint8_t ip, ip1, ip2, ip3;
+  uint8_t padding[4];
+} ea_hq;
+typedef struct {
+  uint64_t s[4];
+  uint64_t t, final;
+} ea_xoshiro;
+
+/* All generator state of a job (Init_Random, PROGRAM/src/ini.c:61-101). */
+typedef struct {
+  ea_hq prc[64];            /* Parisi-Rapuano per replica, feeds the Philox counters */
+  ea_xoshiro xo[64];        /* xoshiro256++ per replica */
+  uint32_t keys[64];        /* Philox key word per replica */
+  ea_hq rc;                 /* random_c: Houdayer replica choice */
+  uint64_t cuda_rng_offset; /* uniforms consumed by the cluster moves so far */
+  uint64_t seed_cluster;    /* cuRAND XORWOW seed */
+} ea_generators;
+
+/* Cadence of one bin (input file fields, PROGRAM/src/io.c:399-436). */
+typedef struct {
+  int32_t itmax, houfr, mesfr, ptfr;
+  int32_t cluster;   /* 0 = NO_CLUSTER build of the reference */
+  int32_t nclust;    /* beta indices (coldest first) in the Houdayer move; <=0: lround(0.5*NB) */
+} ea_cadence;
+
+const char *ea_last_error(void);
+int ea_version(void);
+
+/* ---- host-side set-up (no GPU involved) -------------------------------------
+ * Seeds, couplings and initial spins exactly as the reference builds them. */
+
+/* generate_seed_vectors + Init_Random (ini.c:32-101): per-sample seeds_J/seeds_u,
+ * per-replica seeds_MC, and every generator state.  list_samples may be NULL
+ * (0..nsamples-1).  pt_out: [nsamples][NR] states of the PT generators. */
+int ea_host_seeds(uint64_t master_J, uint64_t master_u, uint64_t master_MC, uint64_t master_cluster,
+                  const int32_t *list_samples, int32_t nsamples, int32_t nrep,
+                  uint64_t *seeds_J, uint64_t *seeds_u, uint64_t *seeds_MC);
+int ea_host_generators(const uint64_t *seeds_MC, const int32_t *list_samples, int32_t nsamples,
+                       int32_t nrep, uint64_t seed_cluster, ea_generators *gen, ea_hq *pt_out);
+/* Init_u + packing_u (ini.c:316-383). even/odd: [NB][half][NR]. */
+int ea_host_init_spins(const ea_geom *g, uint64_t seed_u, uint64_t *even, uint64_t *odd);
+/* Init_J + packing_J (ini.c:465-730).  J6 (may be NULL): the six V-byte planes
+ * Jx,Jy,Jz,Jmx,Jmy,Jmz written to couplings.bin (io.c:284-305).  Jw: [2][6][half]. */
+int ea_host_init_couplings(const ea_geom *g, uint64_t seed_J, uint8_t *J6, uint64_t *Jw, int32_t *countJ);
+/* unpacking_u / packing_u for one replica: spins of every clone as bytes [NB][V] in
+ * natural site order x + L*y + L*L*z (ini.c:385-433). */
+int ea_host_unpack_replica(const ea_geom *g, const uint64_t *even, const uint64_t *odd, int32_t rep, uint8_t *u);
+int ea_host_pack_replica(const ea_geom *g, const uint8_t *u, int32_t rep, uint64_t *even, uint64_t *odd);
+/* calculate_scalar_energy (med.c:3-44) of one clone given as V bytes. */
+int ea_host_scalar_energy(const ea_geom *g, const uint8_t *u, const uint8_t *J6, int32_t *E);
+
+/* ---- device context ------------------------------------------------------------ */
+typedef struct ea_ctx ea_ctx;
+
+/* Allocates the job on `device` (cudaSetDevice + cudaMalloc once, here). */
+int ea_create(const ea_geom *g, int32_t device, ea_ctx **out);
+int ea_destroy(ea_ctx *ctx);
+int ea_get_geom(const ea_ctx *ctx, ea_geom *g);
+int ea_sync(ea_ctx *ctx);
+/* The context's CUDA stream (a cudaStream_t), so callers can order their own
+ * work or timing events with the job's kernels. */
+int ea_get_stream(ea_ctx *ctx, void **stream);
+
+/* Inputs.  betas descending (read_betas, io.c:476-501); cum: [NB][256] (read_lut, io.c:504-534). */
+int ea_set_temperatures(ea_ctx *ctx, const double *betas, const uint64_t *cum);
+int ea_set_spins(ea_ctx *ctx, int32_t sample, const uint64_t *even, const uint64_t *odd);
+int ea_get_spins(ea_ctx *ctx, int32_t sample, uint64_t *even, uint64_t *odd);
+int ea_set_couplings(ea_ctx *ctx, int32_t sample, const uint64_t *Jw);
+/* pt: [nsamples][NR] PT generators (random_PT, header.h:133). */
+int ea_set_generators(ea_ctx *ctx, const ea_generators *gen, const ea_hq *pt);
+int ea_get_generators(ea_ctx *ctx, ea_generators *gen, ea_hq *pt);
+/* which_clon_this_beta [nsamples][NR][NB]; NULL = identity (init_tempering, ini.c:763-781). */
+int ea_set_permutations(ea_ctx *ctx, const uint8_t *wctb);
+int ea_get_permutations(ea_ctx *ctx, uint8_t *wctb, uint8_t *wbtc);
+/* PT acceptance accumulators [nsamples][NR][NB-1] (aceptancePT, attemptsPT, aceptancePTraw). */
+int ea_get_pt_stats(ea_ctx *ctx, double *acc, double *att, double *accraw);
+int ea_reset_pt_stats(ea_ctx *ctx);
+/* Philox time counter and 14-bit job id (main.cu:59-62,139; fill_bits.h:47-68). */
+int ea_set_counter(ea_ctx *ctx, int64_t iter, uint32_t jobid);
+int ea_get_counter(ea_ctx *ctx, int64_t *iter);
+
+/* ---- the hot path ------------------------------------------------------------------ */
+/* Monte_Carlo (main.cu:285-349): nsweeps x {even, odd} half-sweeps of the fused
+ * heat-bath-LUT + Metropolis kernel.  The energies of the final state are
+ * accumulated inside the last odd half-sweep (consumed by ea_parallel_tempering). */
+int ea_monte_carlo(ea_ctx *ctx, int32_t nsweeps);
+/* Measure_Energy (main.cu:531-554).  out may be NULL (result stays on the device). */
+int ea_measure_energy(ea_ctx *ctx, int32_t *out);
+/* Parallel_Tempering for every (sample, replica) (upd.c:3-48) on the device, with
+ * the reference's FP64 arithmetic and glibc exp() values tabulated on the host. */
+int ea_parallel_tempering(ea_ctx *ctx);
+/* Houdayer (main.cu:351-453 + HoudayerXEA.cu): two replica groups, cuRAND XORWOW
+ * uniforms with the reference's seed/offset/sizes, min-index cluster roots. */
+int ea_houdayer(ea_ctx *ctx, int32_t nclust);
+/* One bin (main.cu:149-230): itmax x mesfr x (houfr x (MC + energy + PT) + Houdayer),
+ * then the per-it energy measure, average and temperature-history record.
+ * avgE [nsamples][NR][NB] (sum over it, beta order) and hist [nsamples][NR][maxit][NB]
+ * may be NULL; maxit_trw = itmax / frecTRW (io.c:431-434). */
+int ea_run_bin(ea_ctx *ctx, const ea_cadence *cad, double *avgE, uint8_t *hist, int32_t *maxit_trw);
+
+/* Per-kernel timing: while enabled, every launch of the listed kernels is
+ * bracketed by CUDA events on the context's stream.  ea_kernel_time syncs and
+ * returns the number of launches and their summed duration since enabling. */
+enum { EA_K_SWEEP = 0, EA_K_PT = 1, EA_K_CLUSTER = 2, EA_K_ENERGY = 3, EA_K_COUNT = 4 };
+int ea_profile(ea_ctx *ctx, int32_t on);
+int ea_kernel_time(ea_ctx *ctx, int32_t kind, int64_t *launches, double *total_ms);
+
+/* cuRAND XORWOW uniforms (device generator) for a seed/offset, copied to host.
+ * Used to check the device generator against the host one. */
+int ea_curand_uniforms(int32_t device, uint64_t seed, uint64_t offset, uint64_t n, double *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -770,12 +770,14 @@ int or_run_bin(or_state *st, const or_run_cfg *cfg, uint64_t *iter) {
           int r1, r2;
           or_houdayer_pair(&st->rc, NR, gi, &r1, &r2);
 #ifdef OR_HAVE_CURAND
-          curandGenerator_t gen;
-          if (curandCreateGeneratorHost(&gen, CURAND_RNG_PSEUDO_DEFAULT) != CURAND_STATUS_SUCCESS) { free(ctr); free(U); return -2; }
-          curandSetPseudoRandomGeneratorSeed(gen, (unsigned long long)st->seed_cluster);
-          if (st->cuda_rng_offset > 0) curandSetGeneratorOffset(gen, st->cuda_rng_offset);
-          if (curandGenerateUniformDouble(gen, U, totrandom) != CURAND_STATUS_SUCCESS) { curandDestroyGenerator(gen); free(ctr); free(U); return -2; }
-          curandDestroyGenerator(gen);
+          if (!st->curand_gen) {
+            curandGenerator_t gen;
+            if (curandCreateGeneratorHost(&gen, CURAND_RNG_PSEUDO_DEFAULT) != CURAND_STATUS_SUCCESS) { free(ctr); free(U); return -2; }
+            curandSetPseudoRandomGeneratorSeed(gen, (unsigned long long)st->seed_cluster);
+            if (st->cuda_rng_offset > 0) curandSetGeneratorOffset(gen, st->cuda_rng_offset);
+            st->curand_gen = (void *)gen;
+          }
+          if (curandGenerateUniformDouble((curandGenerator_t)st->curand_gen, U, totrandom) != CURAND_STATUS_SUCCESS) { free(ctr); free(U); return -2; }
 #else
           free(ctr); free(U); return -2;
 #endif
@@ -802,4 +804,28 @@ int or_run_bin(or_state *st, const or_run_cfg *cfg, uint64_t *iter) {
   }
   free(ctr); free(U);
   return 0;
+}
+
+/* cuRAND XORWOW host generator (the library the reference calls on the device,
+ * HoudayerXEA.cu:174-178,189): n uniform doubles at seed/offset. */
+int or_curand_host(uint64_t seed, uint64_t offset, uint64_t n, double *out) {
+#ifdef OR_HAVE_CURAND
+  curandGenerator_t gen;
+  if (curandCreateGeneratorHost(&gen, CURAND_RNG_PSEUDO_DEFAULT) != CURAND_STATUS_SUCCESS) return -2;
+  curandSetPseudoRandomGeneratorSeed(gen, (unsigned long long)seed);
+  if (offset) curandSetGeneratorOffset(gen, offset);
+  curandStatus_t s = curandGenerateUniformDouble(gen, out, n);
+  curandDestroyGenerator(gen);
+  return s == CURAND_STATUS_SUCCESS ? 0 : -2;
+#else
+  (void)seed; (void)offset; (void)n; (void)out;
+  return -2;
+#endif
+}
+
+void or_state_release(or_state *st) {
+#ifdef OR_HAVE_CURAND
+  if (st->curand_gen) curandDestroyGenerator((curandGenerator_t)st->curand_gen);
+#endif
+  st->curand_gen = NULL;
 }

@@ -142,12 +142,20 @@ typedef struct {
   double *betas;            /* [NB] */
   uint64_t *cum;            /* [NB][256] */
   int frec_trw, maxit_trw;
+  /* cuRAND host generator, created at the first cluster move with
+   * (seed_cluster, cuda_rng_offset) and then kept, as the reference keeps its
+   * device generator for the life of the process (HoudayerXEA.cu:174-178).
+   * A fresh generator at offset n does not continue one that produced n numbers. */
+  void *curand_gen;
 } or_state;
+
+void or_state_release(or_state *st);
 
 /* Advance one bin (the body of the ibin loop, main.cu:142-230): Monte Carlo,
  * energy, PT, Houdayer, averages and history.  *iter is the half-sweep counter.
  * Uniforms are drawn with the cuRAND host XORWOW generator (seed, offset). */
 int or_run_bin(or_state *st, const or_run_cfg *cfg, uint64_t *iter);
+int or_curand_host(uint64_t seed, uint64_t offset, uint64_t n, double *out);
 
 #ifdef __cplusplus
 }

