@@ -121,6 +121,11 @@ int set_device(ea_ctx *c) {
 
 }  // namespace
 
+namespace eagb {
+// Lets other translation units of the library report through ea_last_error().
+void set_last_error(const char *msg) { g_err = msg; }
+}  // namespace eagb
+
 static void prof_collect(ea_ctx *c) {
   for (int k = 0; k < EA_K_COUNT; ++k) {
     for (auto &p : c->prof_ev[k]) {

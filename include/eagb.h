@@ -145,6 +145,25 @@ int ea_get_counter(ea_ctx *ctx, int64_t *iter);
 int ea_monte_carlo(ea_ctx *ctx, int32_t nsweeps);
 /* Measure_Energy (main.cu:531-554).  out may be NULL (result stays on the device). */
 int ea_measure_energy(ea_ctx *ctx, int32_t *out);
+/* Energy measurement that allocates nothing.  No counterpart in the reference:
+ * it exists for callers that cannot call cudaMalloc -- code recording into a
+ * CUDA graph while a stream capture is active, frameworks that hand out every
+ * device byte from their own pool, and loops that cannot take the device
+ * synchronisation of an allocation.  Same result as ea_measure_energy for
+ * spins [nsamples][2][NB][half][NR] and couplings [nsamples][2][6][half]
+ * already in device memory; writes energies [nsamples][NR][NB] (int32) to
+ * d_energies on `stream` (a cudaStream_t, NULL = legacy default stream), on
+ * the calling thread's current device.  Its scratch is a fixed 4.4 MiB device
+ * array inside the library (held by every GPU that loads it until exit), so
+ * it rejects, with EA_ERR_ARG and a message, jobs beyond
+ * (L/4)^2 (Lz/4) / 2 <= 8192 half-sites and
+ * ceil(half/KT) * nsamples * NB * NR <= 2^20 partial sums (KT = 32/NR).
+ * The first call on each device looks up the array's device address; make
+ * that first call before any stream capture.  All calls share the array, so
+ * calls whose kernels overlap on the GPU race; serialise them (one stream, or
+ * events).  Nothing in the array needs to start at zero. */
+int ea_measure_energy_noalloc(const ea_geom *g, const uint64_t *d_spins, const uint64_t *d_couplings,
+                              int32_t *d_energies, void *stream);
 /* Parallel_Tempering for every (sample, replica) (upd.c:3-48) on the device, with
  * the reference's FP64 arithmetic and glibc exp() values tabulated on the host. */
 int ea_parallel_tempering(ea_ctx *ctx);
