@@ -2,8 +2,8 @@
 """Throughput of the EA-LCD-MC hot path on one GB300 (spin updates per picosecond).
 
 Workload (one job, reference layout): L=24, Lz=192 tube (110,592 sites), OBC
-along z, NB=32 temperatures uniform in T in [0.6, 1.6], NR=8 replicas, 32
-disorder samples; Metropolis + energy + parallel tempering every sweep and a
+along z, NB=32 temperatures uniform in T in [0.6, 1.6], NR=8 replicas, 31
+disorder samples (the most one reference process takes); Metropolis + energy + parallel tempering every sweep and a
 Houdayer move on the colder half every 5 sweeps.  One step = 5 x (sweep +
 energy + PT) + 1 Houdayer move = 5 * V * NR * NB * 32 spin updates.
 
@@ -27,10 +27,10 @@ import time
 import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
-L, LZ, NR, NS, HOUFR = 24, 192, 8, 32, 5
+L, LZ, NR, NS, HOUFR = 24, 192, 8, 31, 5
 LUT = os.path.join(ROOT, "tests", "golden", "lut_T06_16_N32.npz")
 MASTERS = (0x1234567890ABCDEF, 0x0FEDCBA987654321, 0x1111222233334444, 0x5555666677778888)
-WORKLOAD = "L24_Lz192_OBC_NB32_NR8_ns32_ptfr1_houfr5"
+WORKLOAD = "L24_Lz192_OBC_NB32_NR8_ns31_ptfr1_houfr5"
 
 
 def load_eagb():

@@ -261,6 +261,7 @@ int ea_create(const ea_geom *gp, int32_t device, ea_ctx **out) {
   j.NB = g.NB; j.NR = g.NR; j.ns = g.ns; j.half = g.half; j.msc_l = g.msc_l; j.msc_s = g.msc_s;
   j.msc_lz = g.msc_lz; j.L = g.L; j.Lz = g.Lz; j.V = g.V; j.bc = g.bc; j.kt = kt;
   j.ntiles = (g.half + kt - 1) / kt;
+  j.cc_xq = (int)(((1ULL << 32) - 1 + (uint64_t)g.L) % (uint64_t)g.L);
   const size_t nsr = (size_t)g.ns * g.NR;
 #define OWN(p, n) if ((rc = own(c, p, n)) != EA_OK) { ea_destroy(c); return rc; }
   OWN(j.spins, g.ns * g.words_per_sample());
@@ -628,6 +629,13 @@ static int houdayer(ea_ctx *c, int nclust) {
     prof_end(c, EA_K_CLUSTER, b);
   }
   c->energies_fresh = false;
+  return EA_OK;
+}
+
+int ea_set_cluster_rule(ea_ctx *c, int32_t rule) {
+  if (check(c) || (rule != EA_CLUSTER_REFERENCE && rule != EA_CLUSTER_EXACT)) return fail(EA_ERR_ARG, "bad cluster rule");
+  const int L = c->g.L;
+  c->j.cc_xq = rule == EA_CLUSTER_EXACT ? L - 1 : (int)(((1ULL << 32) - 1 + (uint64_t)L) % (uint64_t)L);
   return EA_OK;
 }
 

@@ -438,7 +438,9 @@ __global__ void k_cc_union(JobDev j) {
   uint32_t *lab = j.label + lat * j.V;
   const int q = q_bit(j, Q, x, y, z);
   const int xm = x == 0 ? L - 1 : x - 1, ym = y == 0 ? L - 1 : y - 1;
-  if (q_bit(j, Q, xm, y, z) == q) cc_unite(lab, (uint32_t)i, (uint32_t)(xm + L * y + S * z));
+  // site 0 tests its x-wrap bond against x = cc_xq (see JobDev::cc_xq)
+  const int xt = i == 0 ? j.cc_xq : xm;
+  if (q_bit(j, Q, xt, y, z) == q) cc_unite(lab, (uint32_t)i, (uint32_t)(xm + L * y + S * z));
   if (q_bit(j, Q, x, ym, z) == q) cc_unite(lab, (uint32_t)i, (uint32_t)(x + L * ym + S * z));
   if (z == 0 && j.bc == EA_PBC && q_bit(j, Q, x, y, j.Lz - 1) == q)
     cc_unite(lab, (uint32_t)i, (uint32_t)(x + L * y + S * (j.Lz - 1)));

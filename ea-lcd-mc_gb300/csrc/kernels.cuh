@@ -44,6 +44,11 @@ struct JobDev {
   uint32_t *label;                  // [s][nclust][V]
   const double *U;                  // [s][NB][V] uniforms of the current group
   int nclust;
+  // x coordinate against which site 0 tests its periodic -x bond.  The
+  // reference computes (ltid-1+nx)%nx with a 32-bit ltid (HoudayerXEA.cu:96),
+  // i.e. (2^32-1+L) mod L, which differs from L-1 unless L is a power of two;
+  // the union itself still joins sites 0 and L-1 (HoudayerXEA.cu:288).
+  int cc_xq;
 };
 
 // Tile width (half-sites per CTA) of the fused sweep kernel.

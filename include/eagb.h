@@ -170,6 +170,14 @@ int ea_parallel_tempering(ea_ctx *ctx);
 /* Houdayer (main.cu:351-453 + HoudayerXEA.cu): two replica groups, cuRAND XORWOW
  * uniforms with the reference's seed/offset/sizes, min-index cluster roots. */
 int ea_houdayer(ea_ctx *ctx, int32_t nclust);
+/* Bond rule of the cluster labelling.  EA_CLUSTER_REFERENCE (default)
+ * reproduces the reference binary: site 0 tests its periodic -x bond against
+ * x = (2^32-1+L) mod L (a 32-bit wrap in HoudayerXEA.cu:96) while still joining
+ * sites 0 and L-1; it equals the correct rule when L is a power of two.
+ * EA_CLUSTER_EXACT tests the bond against x = L-1, so every move conserves
+ * E(r1)+E(r2) for every L. */
+enum { EA_CLUSTER_REFERENCE = 0, EA_CLUSTER_EXACT = 1 };
+int ea_set_cluster_rule(ea_ctx *ctx, int32_t rule);
 /* One bin (main.cu:149-230): itmax x mesfr x (houfr x (MC + energy + PT) + Houdayer),
  * then the per-it energy measure, average and temperature-history record.
  * avgE [nsamples][NR][NB] (sum over it, beta order) and hist [nsamples][NR][maxit][NB]

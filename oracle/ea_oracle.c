@@ -640,17 +640,23 @@ static uint32_t uf_find(uint32_t *par, uint32_t i) {
  * joined to their -x, -y (periodic) and -z neighbours (periodic under PBC, no
  * wrap under OBC) when the overlap bits agree.  Komura's labelling ends with
  * every site pointing at the smallest index of its cluster. */
-void or_cluster_roots(const or_geom *g, const uint8_t *q, uint32_t *root) {
+void or_cluster_roots(const or_geom *g, const uint8_t *q, uint32_t *root, int ref_quirk) {
   const int L = g->L, Lz = g->Lz, S = L * L, V = g->V;
+  /* HoudayerXEA.cu:96 forms (ltid-1+nx)%nx with a 32-bit ltid, so for site 0
+   * the x-wrap bond is tested against site (2^32-1+L) mod L, while the union
+   * (HoudayerXEA.cu:288, 64-bit index) still joins site 0 with site L-1. */
+  const int xq = (int)(((1ULL << 32) - 1 + (uint64_t)L) % (uint64_t)L);
   for (int i = 0; i < V; i++) root[i] = (uint32_t)i;
   for (int i = 0; i < V; i++) {
     int x = i % L, y = (i / L) % L, z = i / S;
-    int nb[3];
+    int nb[3], tst[3];
     nb[0] = (x == 0 ? L - 1 : x - 1) + y * L + z * S;
     nb[1] = x + (y == 0 ? L - 1 : y - 1) * L + z * S;
     nb[2] = (g->bc != OR_PBC && z == 0) ? -1 : x + y * L + (z == 0 ? Lz - 1 : z - 1) * S;
+    tst[0] = (i == 0 && ref_quirk) ? xq : nb[0];
+    tst[1] = nb[1]; tst[2] = nb[2];
     for (int d = 0; d < 3; d++) {
-      if (nb[d] < 0 || q[nb[d]] != q[i]) continue;
+      if (nb[d] < 0 || q[tst[d]] != q[i]) continue;
       uint32_t a = uf_find(root, (uint32_t)i), b = uf_find(root, (uint32_t)nb[d]);
       if (a < b) root[b] = a; else if (b < a) root[a] = b;
     }
@@ -661,7 +667,7 @@ void or_cluster_roots(const or_geom *g, const uint8_t *q, uint32_t *root) {
 /* d_computeoverlap + d_unpack + ClusterStep + d_pack + d_useoverlap,
  * main.cu:776-991 and HoudayerXEA.cu:54-75,183-211,358-374 */
 void or_houdayer_group(const or_geom *g, uint64_t *spins, const uint8_t *wctb, int r1, int r2,
-                       const double *U, int nclust) {
+                       const double *U, int nclust, int ref_quirk) {
   const int NB = g->NB, NR = g->NR, half = g->half, V = g->V;
   const size_t nwc = (size_t)half * NR, nwp = nwc * NB;
   uint8_t *q = (uint8_t *)malloc((size_t)V);
@@ -680,7 +686,7 @@ void or_houdayer_group(const or_geom *g, uint64_t *spins, const uint8_t *wctb, i
       }
       or_unpack_spins(&g1, qe, qo, qu);
       memcpy(q, qu, (size_t)V);
-      or_cluster_roots(g, q, root);
+      or_cluster_roots(g, q, root, ref_quirk);
       const double *Ub = U + ((size_t)s * NB + b) * V;
       for (int i = 0; i < V; i++) qu[i] = q[i] ^ (uint8_t)(Ub[root[i]] < 0.5);
       or_pack_spins(&g1, qu, qe, qo);
@@ -782,7 +788,7 @@ int or_run_bin(or_state *st, const or_run_cfg *cfg, uint64_t *iter) {
           free(ctr); free(U); return -2;
 #endif
           st->cuda_rng_offset += totrandom;
-          or_houdayer_group(g, st->spins, st->wctb, r1, r2, U, cfg->nclust);
+          or_houdayer_group(g, st->spins, st->wctb, r1, r2, U, cfg->nclust, !cfg->cluster_exact);
         }
       }
     }

@@ -107,9 +107,10 @@ void or_houdayer_pair(or_hq *rc, int NR, int g, int *r1, int *r2);
  * sample.  U: [nbits][NB][V] uniforms of this cluster step.  nclust: number of
  * beta indices (coldest first) that take part (lround(0.5*NB) in the reference). */
 void or_houdayer_group(const or_geom *g, uint64_t *spins, const uint8_t *wctb, int r1, int r2,
-                       const double *U, int nclust);
-/* Labels only (for tests): root[V] = minimum site index of the equal-q cluster. */
-void or_cluster_roots(const or_geom *g, const uint8_t *q /*[V]*/, uint32_t *root);
+                       const double *U, int nclust, int ref_quirk);
+/* Labels only (for tests): root[V] = minimum site index of the equal-q cluster.
+ * ref_quirk != 0 reproduces the reference's test of site 0's x-wrap bond. */
+void or_cluster_roots(const or_geom *g, const uint8_t *q /*[V]*/, uint32_t *root, int ref_quirk);
 
 /* ---- LUT (create_LUT.c) ----------------------------------------------------- */
 /* Cumulative thresholds and the reference file layout of one beta.  Returns 0 on
@@ -124,6 +125,7 @@ typedef struct {
   int cluster;     /* 0: NO_CLUSTER */
   int nclust;      /* beta indices in the Houdayer move */
   int nthreads;
+  int cluster_exact; /* 1: test site 0's x-wrap bond correctly (not the reference's behaviour) */
 } or_run_cfg;
 
 /* Complete mutable state of a run (host view). */

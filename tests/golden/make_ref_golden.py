@@ -45,42 +45,23 @@ CASES = {
     "r6_L24_Lz192_OBC_NB32": (24, 192, "OBC", 1, "T06_16_N32", 2, 2, None, 1, 1, 5, 1, 1, 0),
 }
 # timing runs of the reference binary (same geometry as bench.py): tag, nbits, nbin, itmax, houfr
-TIMING = [("t1_L24_Lz192_OBC_NB32_ns32", 32, 2, 20, 5)]
+TIMING = {"t1_L24_Lz192_OBC_NB32_ns31": (31, 2, 20, 5)}
 
 
-def lut_file(name, path):
-    d = np.load(os.path.join(HERE, "lut_%s.npz" % name))
-    betas = d["betas"]
-    nb = len(betas)
-    raw = betas.astype(np.float64).tobytes()
+def case_inputs(tag, dirpath):
+    """Write the input files of case `tag` into dirpath (LUT rebuilt from the
+    committed thresholds and checked against the generator's file digest)."""
     sys.path.insert(0, os.path.dirname(HERE))
-    import oracle_py
-    for b in betas:
-        cum, umb, pre = oracle_py.lut_beta(float(b))
-        raw += umb.tobytes() + pre.tobytes()
-    assert hashlib.sha256(raw).digest() == d["file_sha256"].tobytes()
-    with open(path, "wb") as f:
-        f.write(raw)
-    return betas
-
-
-def write_case(tag, L, Lz, lutname, nbits, lst, nbin, itmax, houfr, mesfr, ptfr, flag=1):
-    d = os.path.join(RUNS, tag)
-    os.makedirs(d, exist_ok=True)
-    betas = lut_file(lutname, os.path.join(d, "LUT"))
-    with open(os.path.join(d, "betas"), "w") as f:
-        for b in betas:
-            f.write("%.17g\n" % b)
-    with open(os.path.join(d, "input.in"), "w") as f:
-        f.write("./\n")
-        for v in (nbin, 0, itmax, houfr, mesfr, ptfr, len(betas), flag, (Lz << 16) | L):
-            f.write("%d\n" % v)
-        for m in MASTERS:
-            f.write("%d\n" % m)
-    if lst:
-        with open(os.path.join(d, "list"), "w") as f:
-            f.write("\n".join(str(x) for x in lst) + "\n")
-    return len(betas)
+    import refflow
+    if tag in CASES:
+        L, Lz, BC, cl, lutname, isample, nbits, lst, nbin, itmax, houfr, mesfr, ptfr, resume = CASES[tag]
+    else:
+        (nbits, nbin, itmax, houfr), (L, Lz, lutname, lst, mesfr, ptfr) = TIMING[tag], (24, 192, "T06_16_N32", None, 1, 1)
+    d = np.load(os.path.join(HERE, "lut_%s.npz" % lutname))
+    assert hashlib.sha256(refflow.lut_bytes(d["betas"], d["cum"])).digest() == d["file_sha256"].tobytes()
+    refflow.write_case_inputs(dirpath, L, Lz, d["betas"], d["cum"], nbits, lst, nbin, itmax, houfr, mesfr, ptfr,
+                              MASTERS)
+    return len(d["betas"])
 
 
 def stage():
@@ -93,14 +74,14 @@ def stage():
              "nvidia-smi -L > gpurun_out/refgold/gpu.txt 2>&1", "builds=()"]
     runs = []
     for tag, (L, Lz, BC, cl, lutname, isample, nbits, lst, nbin, itmax, houfr, mesfr, ptfr, resume) in CASES.items():
-        nb = write_case(tag, L, Lz, lutname, nbits, lst, nbin, itmax, houfr, mesfr, ptfr)
+        nb = case_inputs(tag, os.path.join(RUNS, tag))
         cfg = "%d,%d,%d,%s" % (L, Lz, nb, BC)
         exe = "oracle/_ref/bin/EA_L%d_Lz%d_NB%d_%s%s" % (L, Lz, nb, BC, "" if cl else "_NOCL")
         lines.append("make -s -C oracle ref-cuda CFG=%s CLUSTER=%d > gpurun_out/refgold/build_%s.log 2>&1 &" % (cfg, cl, tag))
         args = "%d %d betas input.in LUT 0 0%s" % (isample, nbits, " list" if lst else "")
         runs.append((tag, exe, args, resume))
-    for tag, nbits, nbin, itmax, houfr in TIMING:
-        nb = write_case(tag, 24, 192, "T06_16_N32", nbits, None, nbin, itmax, houfr, 1, 1)
+    for tag, (nbits, nbin, itmax, houfr) in TIMING.items():
+        nb = case_inputs(tag, os.path.join(RUNS, tag))
         runs.append((tag, "oracle/_ref/bin/EA_L24_Lz192_NB%d_OBC" % nb, "0 %d betas input.in LUT 0 0" % nbits, 0))
     lines.append("wait")
     for tag, exe, args, resume in runs:
@@ -124,11 +105,12 @@ def collect():
         for dp, _, files in os.walk(base):
             for fn in sorted(files):
                 rel = os.path.relpath(os.path.join(dp, fn), base)
-                if rel in ("LUT",) or rel.startswith(("running", "time.log")) or "run.log" in rel and "/" in rel:
+                # `conf` is a hard link to the newest conf.%06d (io.c:73-86)
+                if fn in ("LUT", "conf") or fn.startswith(("running", "time.log")):
                     continue
                 raw = open(os.path.join(dp, fn), "rb").read()
                 key = rel.replace("/", "|")
-                if len(raw) <= 262144:
+                if len(raw) <= 65536:
                     out["file:" + key] = np.frombuffer(raw, np.uint8).copy()
                 else:
                     out["sha256:" + key] = np.frombuffer(hashlib.sha256(raw).digest(), np.uint8)

@@ -40,7 +40,7 @@ class Seeds(C.Structure):
 class RunCfg(C.Structure):
     _fields_ = [("nbin", C.c_int), ("itcut", C.c_int), ("itmax", C.c_int), ("houfr", C.c_int),
                 ("mesfr", C.c_int), ("ptfr", C.c_int), ("jobid", C.c_uint32), ("cluster", C.c_int),
-                ("nclust", C.c_int), ("nthreads", C.c_int)]
+                ("nclust", C.c_int), ("nthreads", C.c_int), ("cluster_exact", C.c_int)]
 
 
 P = C.c_void_p
@@ -233,10 +233,11 @@ class Sim:
         return st
 
     def run_bin(self, itmax, houfr, mesfr, ptfr, iter0, jobid=0, cluster=True, nclust=None,
-                nthreads=0):
+                nthreads=0, cluster_exact=False):
         st = self.state()
         cfg = RunCfg(1, 0, itmax, houfr, mesfr, ptfr, jobid, int(cluster),
-                     nclust if nclust is not None else int(np.floor(self.g.NB * 0.5 + 0.5)), nthreads)
+                     nclust if nclust is not None else int(np.floor(self.g.NB * 0.5 + 0.5)), nthreads,
+                     int(cluster_exact))
         it = C.c_uint64(iter0)
         rc = lib().or_run_bin(C.byref(st), C.byref(cfg), C.byref(it))
         if rc != 0:
