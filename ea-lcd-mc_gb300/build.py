@@ -50,6 +50,14 @@ def build(verbose=False):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed: %s\n%s" % (" ".join(cmd), r.stderr))
+    exe = os.path.join(HERE, "ea_gb")
+    src = os.path.join(CSRC, "ea_gb.cpp")
+    if not os.path.exists(exe) or os.path.getmtime(exe) < max(os.path.getmtime(LIB), os.path.getmtime(src)):
+        cmd = ["g++", "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"), src, "-o", exe,
+               "-L" + HERE, "-leagb", "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("driver build failed: %s\n%s" % (" ".join(cmd), r.stderr))
     if verbose:
         for o in objs:
             if os.path.exists(o + ".log"):

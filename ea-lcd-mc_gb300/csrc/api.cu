@@ -147,6 +147,14 @@ extern "C" {
 const char *ea_last_error(void) { return g_err.c_str(); }
 int ea_version(void) { return EA_VERSION; }
 
+int ea_device_count(int32_t *count) {
+  if (!count) return fail(EA_ERR_ARG, "null argument");
+  int n = 0;
+  CU(cudaGetDeviceCount(&n));
+  *count = n;
+  return EA_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Host-side set-up
 // ---------------------------------------------------------------------------

@@ -84,6 +84,8 @@ typedef struct {
 
 const char *ea_last_error(void);
 int ea_version(void);
+/* Number of visible CUDA devices (cudaGetDeviceCount, main.cu:64). */
+int ea_device_count(int32_t *count);
 
 /* ---- host-side set-up (no GPU involved) -------------------------------------
  * Seeds, couplings and initial spins exactly as the reference builds them. */
