@@ -409,19 +409,76 @@ __global__ void k_cc_init(JobDev j) {
   j.label[t] = m;
 }
 
+// Lock-free union: the larger of the two roots is hung below the smaller one
+// with atomicMin; when another thread got there first the walk continues from
+// the value it left.  Labels only decrease, so every chain ends at the
+// smallest index of its cluster.  Works on global and shared memory.
 __device__ __forceinline__ void cc_unite(uint32_t *lab, uint32_t a, uint32_t b) {
   uint32_t l1 = cc_find(lab, a), l2 = cc_find(lab, b);
   if (l1 == l2) return;
   if (l1 < l2) { const uint32_t t = l1; l1 = l2; l2 = t; }
   for (;;) {
     const uint32_t l3 = atomicMin(&lab[l1], l2);
-    if (l3 == l2 || l3 == l1) {
-      if (l3 == l1) return;  // l1 was a root and now hangs below l2
-      return;
-    }
+    if (l3 == l2 || l3 == l1) return;  // already joined, or l1 was a root and now hangs below l2
     if (l3 > l2) { l1 = l3; }
     else { l1 = l2; l2 = l3; }
   }
+}
+
+// Slab labelling.  A CTA labels the equal-overlap clusters of D consecutive z
+// planes of one (sample, beta) lattice in SMEM.  Local index order is natural
+// order shifted by z0 L^2, so a slab root is the smallest global index of its
+// slab piece; only bonds between slabs are left for k_cc_merge.
+constexpr int kSlabSites = 8192;
+
+__global__ void __launch_bounds__(512) k_cc_local(JobDev j, int D) {
+  __shared__ uint32_t lab[kSlabSites];
+  __shared__ uint8_t qs[kSlabSites];
+  const int L = j.L, S = L * L, tid = threadIdx.x, nth = blockDim.x;
+  const size_t lat = blockIdx.y;
+  const int z0 = blockIdx.x * D, nz = min(D, j.Lz - z0), n = S * nz;
+  const u64 *Q = j.Q + lat * 2 * j.half;
+  for (int i = tid; i < n; i += nth) {
+    const int x = i % L, y = (i / L) % L, z = z0 + i / S;
+    qs[i] = (uint8_t)q_bit(j, Q, x, y, z);
+    lab[i] = (uint32_t)i;
+  }
+  __syncthreads();
+  for (int i = tid; i < n; i += nth) {
+    const int x = i % L, y = (i / L) % L, zl = i / S, q = qs[i];
+    const int xm = x == 0 ? L - 1 : x - 1, ym = y == 0 ? L - 1 : y - 1;
+    // site 0 tests its x-wrap bond against x = cc_xq (see JobDev::cc_xq)
+    const int xt = (z0 == 0 && i == 0) ? j.cc_xq : xm;
+    if (qs[xt + L * y + S * zl] == q) cc_unite(lab, (uint32_t)i, (uint32_t)(xm + L * y + S * zl));
+    if (qs[x + L * ym + S * zl] == q) cc_unite(lab, (uint32_t)i, (uint32_t)(x + L * ym + S * zl));
+    if (zl > 0 && qs[i - S] == q) cc_unite(lab, (uint32_t)i, (uint32_t)(i - S));
+  }
+  __syncthreads();
+  uint32_t *glab = j.label + lat * j.V + (size_t)z0 * S;
+  const uint32_t off = (uint32_t)z0 * S;
+  for (int i = tid; i < n; i += nth) glab[i] = off + cc_find(lab, (uint32_t)i);
+}
+
+// Bonds across slab faces (z = f D with z - 1), and the z wrap under PBC,
+// merged into the global labels.
+__global__ void k_cc_merge(JobDev j, int D, int nslab) {
+  const int L = j.L, S = L * L;
+  const size_t per_lat = (size_t)nslab * S;
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (size_t)j.ns * j.nclust * per_lat) return;
+  const size_t lat = t / per_lat;
+  const int r = (int)(t % per_lat), f = r / S, xy = r % S;
+  int z, zm;
+  if (f == 0) {
+    if (j.bc != EA_PBC) return;
+    z = 0; zm = j.Lz - 1;
+  } else {
+    z = f * D; zm = z - 1;
+  }
+  const int x = xy % L, y = xy / L;
+  const u64 *Q = j.Q + lat * 2 * j.half;
+  if (q_bit(j, Q, x, y, z) == q_bit(j, Q, x, y, zm))
+    cc_unite(j.label + lat * j.V, (uint32_t)(xy + S * z), (uint32_t)(xy + S * zm));
 }
 
 // Label reduction of Komura (HoudayerXEA.cu:254-331): every bond that is not
@@ -474,7 +531,7 @@ __global__ void k_hou_apply(JobDev j, int g) {
   u64 sel = 0;
   for (int bit = 0; bit < 64; ++bit) {
     const int x = gx + (bit & 3) * j.msc_l, y = gy + ((bit >> 2) & 3) * j.msc_l, z = gz + (bit >> 4) * j.msc_lz;
-    const uint32_t root = lab[x + L * y + S * z];
+    const uint32_t root = cc_find(lab, (uint32_t)(x + L * y + S * z));
     sel |= (u64)(U[root] < 0.5) << bit;
   }
   const u64 qn = j.Q[i] ^ sel;
@@ -567,9 +624,18 @@ cudaError_t launch_houdayer_group(const JobDev &j, int g, cudaStream_t st) {
   const size_t ns = (size_t)j.ns * j.nclust * j.V;
   const unsigned bw = (unsigned)((nw + 255) / 256), bs = (unsigned)((ns + 255) / 256);
   k_hou_overlap<<<bw, 256, 0, st>>>(j, g);
-  k_cc_init<<<bs, 256, 0, st>>>(j);
-  k_cc_union<<<bs, 256, 0, st>>>(j);
-  k_cc_flatten<<<bs, 256, 0, st>>>(j);
+  const int S = j.L * j.L;
+  if (S <= kSlabSites) {
+    const int D = min(j.Lz, kSlabSites / S), nslab = (j.Lz + D - 1) / D;
+    k_cc_local<<<dim3(nslab, j.ns * j.nclust), 512, 0, st>>>(j, D);
+    const size_t nm = (size_t)j.ns * j.nclust * nslab * S;
+    k_cc_merge<<<(unsigned)((nm + 255) / 256), 256, 0, st>>>(j, D, nslab);
+  } else {
+    // planes too large for SMEM: Komura's passes on global labels
+    k_cc_init<<<bs, 256, 0, st>>>(j);
+    k_cc_flatten<<<bs, 256, 0, st>>>(j);
+    k_cc_union<<<bs, 256, 0, st>>>(j);
+  }
   k_hou_apply<<<bw, 256, 0, st>>>(j, g);
   return cudaGetLastError();
 }
