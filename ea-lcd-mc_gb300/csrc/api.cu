@@ -62,7 +62,11 @@ struct ea_ctx {
   curandGenerator_t gen = nullptr;
   uint64_t cuda_rng_offset = 0, seed_cluster = 0;
   int nclust_cap = 0;
-  double *U = nullptr;
+  // uniforms of the two groups of a move.  They are drawn on the job's own
+  // stream: drawn on a second stream overlapping the sweeps, the generator ran
+  // about 4x slower once moves were queued back to back.
+  double *U[2] = {nullptr, nullptr};
+  bool pregen = false;
   uint32_t *label = nullptr;
   unsigned long long *Q = nullptr;
   // measurement buffers
@@ -270,6 +274,7 @@ int ea_create(const ea_geom *gp, int32_t device, ea_ctx **out) {
   j.msc_lz = g.msc_lz; j.L = g.L; j.Lz = g.Lz; j.V = g.V; j.bc = g.bc; j.kt = kt;
   j.ntiles = (g.half + kt - 1) / kt;
   j.cc_xq = (int)(((1ULL << 32) - 1 + (uint64_t)g.L) % (uint64_t)g.L);
+  set_dividers(j);
   const size_t nsr = (size_t)g.ns * g.NR;
 #define OWN(p, n) if ((rc = own(c, p, n)) != EA_OK) { ea_destroy(c); return rc; }
   OWN(j.spins, g.ns * g.words_per_sample());
@@ -317,7 +322,8 @@ int ea_destroy(ea_ctx *c) {
   if (c->gen) curandDestroyGenerator(c->gen);
   prof_collect(c);
   for (void *p : c->owned) cudaFree(p);
-  if (c->U) cudaFree(c->U);
+  for (double *u : c->U)
+    if (u) cudaFree(u);
   if (c->label) cudaFree(c->label);
   if (c->Q) cudaFree(c->Q);
   if (c->hist) cudaFree(c->hist);
@@ -416,6 +422,12 @@ int ea_set_generators(ea_ctx *c, const ea_generators *gen, const ea_hq *pt) {
   CU(cudaMemcpyAsync(c->j.rc, &gen->rc, sizeof(ea_hq), cudaMemcpyHostToDevice, c->st));
   CU(cudaMemcpyAsync(c->j.pt, pt, sizeof(ea_hq) * g.ns * g.NR, cudaMemcpyHostToDevice, c->st));
   CU(cudaStreamSynchronize(c->st));
+  if (c->pregen) {
+    // uniforms drawn ahead for a move that has not run are given back
+    c->cuda_rng_offset -= 2 * (uint64_t)g.V * g.NB * g.ns;
+    c->pregen = false;
+    if (c->gen) { curandDestroyGenerator(c->gen); c->gen = nullptr; }
+  }
   if (c->gen && (gen->seed_cluster != c->seed_cluster || gen->cuda_rng_offset != c->cuda_rng_offset)) {
     curandDestroyGenerator(c->gen);
     c->gen = nullptr;
@@ -517,19 +529,19 @@ int ea_get_counter(ea_ctx *c, int64_t *iter) {
 // Hot path
 // ---------------------------------------------------------------------------
 // Event pair around one launch when profiling is on (ea_profile).
-static cudaEvent_t prof_begin(ea_ctx *c) {
+static cudaEvent_t prof_begin(ea_ctx *c, cudaStream_t st = nullptr) {
   if (!c->prof_on) return nullptr;
   cudaEvent_t e;
   if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
-  cudaEventRecord(e, c->st);
+  cudaEventRecord(e, st ? st : c->st);
   return e;
 }
 
-static void prof_end(ea_ctx *c, int kind, cudaEvent_t b) {
+static void prof_end(ea_ctx *c, int kind, cudaEvent_t b, cudaStream_t st = nullptr) {
   if (!b) return;
   cudaEvent_t e;
   if (cudaEventCreate(&e) != cudaSuccess) return;
-  cudaEventRecord(e, c->st);
+  cudaEventRecord(e, st ? st : c->st);
   c->prof_ev[kind].push_back({b, e});
 }
 
@@ -593,11 +605,10 @@ int ea_parallel_tempering(ea_ctx *c) {
 
 static int ensure_cluster(ea_ctx *c, int nclust) {
   const Geometry &g = c->g;
-  if (!c->U) {
-    CU(dalloc(c->U, (size_t)g.V * g.NB * g.ns));
-    c->j.U = c->U;
-  }
+  for (double *&u : c->U)
+    if (!u) CU(dalloc(u, (size_t)g.V * g.NB * g.ns));
   if (nclust > c->nclust_cap) {
+    CU(cudaStreamSynchronize(c->st));
     if (c->label) cudaFree(c->label);
     if (c->Q) cudaFree(c->Q);
     c->label = nullptr; c->Q = nullptr;
@@ -608,6 +619,7 @@ static int ensure_cluster(ea_ctx *c, int nclust) {
   c->j.label = c->label;
   c->j.Q = c->Q;
   c->j.nclust = nclust;
+  set_dividers(c->j);
   if (!c->gen) {
     // ClusterInit (HoudayerXEA.cu:174-178): default pseudo generator (XORWOW),
     // seed_Cluster, and the offset already consumed.
@@ -619,31 +631,47 @@ static int ensure_cluster(ea_ctx *c, int nclust) {
   return EA_OK;
 }
 
-static int houdayer(ea_ctx *c, int nclust) {
-  const Geometry &g = c->g;
-  if (g.NR < 4) return fail(EA_ERR_ARG, "the Houdayer move needs at least 2 replicas per group");
+static int norm_nclust(const Geometry &g, int nclust) {
   if (nclust <= 0) nclust = (int)std::lround(g.NB * 0.5);
-  if (nclust > g.NB) nclust = g.NB;
-  int rc = ensure_cluster(c, nclust);
+  return nclust > g.NB ? g.NB : nclust;
+}
+
+// ClusterStep's uniforms (HoudayerXEA.cu:189-195) for both groups of a move:
+// V*NB*nsamples doubles per group, in the reference's call sizes.
+static int houdayer_generate(ea_ctx *c, int nclust) {
+  const Geometry &g = c->g;
+  if (c->pregen) return EA_OK;
+  int rc = ensure_cluster(c, norm_nclust(g, nclust));
   if (rc) return rc;
-  CU(launch_houdayer_pairs(c->j, c->st));
   const size_t tot = (size_t)g.V * g.NB * g.ns;
+  cudaEvent_t b = prof_begin(c);
   for (int grp = 0; grp < 2; ++grp) {
-    // ClusterStep (HoudayerXEA.cu:189-195): V*NB*nsamples uniforms per group
-    CR(curandGenerateUniformDouble(c->gen, c->U, tot));
+    CR(curandGenerateUniformDouble(c->gen, c->U[grp], tot));
     c->cuda_rng_offset += tot;
-    cudaEvent_t b = prof_begin(c);
-    CU(launch_houdayer_group(c->j, grp, c->st));
-    prof_end(c, EA_K_CLUSTER, b);
   }
-  c->energies_fresh = false;
+  prof_end(c, EA_K_RNG, b);
+  c->pregen = true;
   return EA_OK;
 }
 
-int ea_set_cluster_rule(ea_ctx *c, int32_t rule) {
-  if (check(c) || (rule != EA_CLUSTER_REFERENCE && rule != EA_CLUSTER_EXACT)) return fail(EA_ERR_ARG, "bad cluster rule");
-  const int L = c->g.L;
-  c->j.cc_xq = rule == EA_CLUSTER_EXACT ? L - 1 : (int)(((1ULL << 32) - 1 + (uint64_t)L) % (uint64_t)L);
+static int houdayer(ea_ctx *c, int nclust) {
+  const Geometry &g = c->g;
+  if (g.NR < 4) return fail(EA_ERR_ARG, "the Houdayer move needs at least 2 replicas per group");
+  nclust = norm_nclust(g, nclust);
+  int rc = houdayer_generate(c, nclust);
+  if (rc) return rc;
+  rc = ensure_cluster(c, nclust);
+  if (rc) return rc;
+  CU(launch_houdayer_pairs(c->j, c->st));
+  for (int grp = 0; grp < 2; ++grp) {
+    JobDev jg = c->j;
+    jg.U = c->U[grp];
+    cudaEvent_t b = prof_begin(c);
+    CU(launch_houdayer_group(jg, grp, c->st));
+    prof_end(c, EA_K_CLUSTER, b);
+  }
+  c->pregen = false;
+  c->energies_fresh = false;
   return EA_OK;
 }
 
@@ -651,6 +679,13 @@ int ea_houdayer(ea_ctx *c, int32_t nclust) {
   if (check(c)) return EA_ERR_ARG;
   if (set_device(c)) return EA_ERR_CUDA;
   return houdayer(c, nclust);
+}
+
+int ea_set_cluster_rule(ea_ctx *c, int32_t rule) {
+  if (check(c) || (rule != EA_CLUSTER_REFERENCE && rule != EA_CLUSTER_EXACT)) return fail(EA_ERR_ARG, "bad cluster rule");
+  const int L = c->g.L;
+  c->j.cc_xq = rule == EA_CLUSTER_EXACT ? L - 1 : (int)(((1ULL << 32) - 1 + (uint64_t)L) % (uint64_t)L);
+  return EA_OK;
 }
 
 static void trw(int itmax, int *frec, int *maxit) {
@@ -691,12 +726,20 @@ int ea_run_bin(ea_ctx *c, const ea_cadence *cad, double *avgE, uint8_t *hist, in
     if ((rc = measure(c))) return rc;
     CU(launch_measure(c->j, (it % frec == frec - 1) ? it / frec : -1, c->st));
   }
+  if (maxit_trw) *maxit_trw = maxit;
+  if (!avgE && !hist) return EA_OK;  // nothing to hand back: stay asynchronous
   if (avgE) CU(cudaMemcpyAsync(avgE, c->avgE, nsr * g.NB * 8, cudaMemcpyDeviceToHost, c->st));
   if (hist) CU(cudaMemcpyAsync(hist, c->hist, nsr * maxit * g.NB, cudaMemcpyDeviceToHost, c->st));
   CU(cudaStreamSynchronize(c->st));
-  if (maxit_trw) *maxit_trw = maxit;
+  return ea_check_exact(c);
+}
+
+int ea_check_exact(ea_ctx *c) {
+  if (check(c)) return EA_ERR_ARG;
+  if (set_device(c)) return EA_ERR_CUDA;
   unsigned long long inex = 0;
-  CU(cudaMemcpy(&inex, c->j.inexact, 8, cudaMemcpyDeviceToHost));
+  CU(cudaMemcpyAsync(&inex, c->j.inexact, 8, cudaMemcpyDeviceToHost, c->st));
+  CU(cudaStreamSynchronize(c->st));
   if (inex) return fail(EA_ERR_INEXACT, "%llu tempering decisions fell outside the exact exp table", inex);
   return EA_OK;
 }

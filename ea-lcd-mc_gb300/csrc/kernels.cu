@@ -157,7 +157,7 @@ __device__ __forceinline__ u64 flip_mask(const u64 f[6], u64 b0, u64 b1, u64 b2)
 // energy of the updated words (each bond has exactly one end on each parity).
 // ---------------------------------------------------------------------------
 template <int NR, int KT, bool UPDATE>
-__global__ void __launch_bounds__(256) k_sweep(JobDev j, int parity, int energy) {
+__global__ void __launch_bounds__(512) k_sweep(JobDev j, int parity, int energy) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int NB = j.NB, half = j.half;
   u64 *s_cum = reinterpret_cast<u64 *>(smem);
@@ -204,27 +204,37 @@ __global__ void __launch_bounds__(256) k_sweep(JobDev j, int parity, int energy)
     __syncthreads();
   }
 
+  // Update phase.  Lanes form groups of G = KT*NR; a lane keeps its
+  // (half-site, replica) and its neighbour record for the whole loop and walks
+  // the (sample, clone) pairs with a stride of one group per iteration, so the
+  // G lanes of a group touch G consecutive words of one clone array.
+  constexpr int G = KT * NR;
   const size_t wpc = (size_t)half * NR, wpp = wpc * NB;
-  const int items = j.ns * NB * KT * NR;
-  const int items32 = (items + 31) & ~31;
+  const int lg = tid % G, grp = tid / G, ngrp = nth / G;
+  const int r = lg % NR, kk = lg / NR, k = k0 + kk;
+  const bool kvalid = k < half;
   const bool obc = j.bc != EA_PBC;
-  for (int i = tid; i < items32; i += nth) {
-    const int r = i % NR, kk = (i / NR) % KT, sc = i / (NR * KT);
-    const int c = sc % NB, s = sc / NB, k = k0 + kk;
-    const bool valid = i < items && k < half;
+  int nb[6];
+#pragma unroll
+  for (int d = 0; d < 6; ++d) nb[d] = s_nb[kk * 8 + d];
+  const int nflags = s_nb[kk * 8 + 6];
+  const int nsc = j.ns * NB, iters = (nsc + ngrp - 1) / ngrp;
+  const int ds = ngrp / NB, dc = ngrp % NB;
+  int s = grp / NB, c = grp % NB;
+  for (int it = 0, sc = grp; it < iters; ++it, sc += ngrp) {
+    const bool valid = kvalid && sc < nsc;
     int e = 0;
     if (valid) {
-      u64 *base = j.spins + (size_t)s * 2 * wpp;
-      u64 *tgt = base + (size_t)parity * wpp + (size_t)c * wpc + (size_t)k * NR + r;
-      const u64 *oth = base + (size_t)(1 - parity) * wpp + (size_t)c * wpc + r;
-      const int *nb = s_nb + kk * 8;
-      u64 n[6];
-      gather6(oth, nb, nb[6], parity, obc, NR, n);
+      u64 *base = j.spins + (size_t)s * 2 * wpp + (size_t)c * wpc;
+      u64 *tgt = base + (size_t)parity * wpp + (size_t)k * NR + r;
+      const u64 *oth = base + (size_t)(1 - parity) * wpp + r;
       const u64 *Jp = j.J + ((size_t)s * 2 + parity) * 6 * half + k;
       const u64 sv = *tgt;
+      u64 n[6];
+      gather6(oth, nb, nflags, parity, obc, NR, n);
       u64 f[6];
 #pragma unroll
-      for (int d = 0; d < 6; ++d) f[d] = sv ^ Jp[(size_t)d * half] ^ n[d];
+      for (int d = 0; d < 6; ++d) f[d] = sv ^ __ldg(Jp + (size_t)d * half) ^ n[d];
       u64 fl = 0;
       if (UPDATE) {
         const int beta = j.wbtc[(s * NR + r) * NB + c];
@@ -241,9 +251,11 @@ __global__ void __launch_bounds__(256) k_sweep(JobDev j, int parity, int energy)
     }
     if (energy) {
 #pragma unroll
-      for (int m = NR; m < KT * NR; m <<= 1) e += __shfl_xor_sync(0xffffffffu, e, m);
+      for (int m = NR; m < G; m <<= 1) e += __shfl_xor_sync(0xffffffffu, e, m);
       if (valid && kk == 0) j.epart[(((size_t)blockIdx.x * j.ns + s) * NB + c) * NR + r] = e;
     }
+    c += dc; s += ds;
+    if (c >= NB) { c -= NB; ++s; }
   }
 }
 
@@ -359,11 +371,11 @@ __global__ void k_hou_pairs(JobDev j) {
 
 // q = s_r1 ^ s_r2 per (sample, beta < nclust, parity, half) (main.cu:889-936).
 __global__ void k_hou_overlap(JobDev j, int g) {
-  const size_t n = (size_t)j.ns * j.nclust * 2 * j.half;
-  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const int k = (int)(i % j.half), p = (int)((i / j.half) & 1);
-  const int b = (int)((i / (2 * (size_t)j.half)) % j.nclust), s = (int)(i / (2 * (size_t)j.half * j.nclust));
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= 2 * j.half) return;
+  const size_t lat = blockIdx.y, i = lat * 2 * j.half + w;
+  const int p = w >= j.half, k = w - p * j.half;
+  const int s = j.fd_nclust.div((uint32_t)lat), b = (int)lat - s * j.nclust;
   const int r1 = j.pairs[2 * g], r2 = j.pairs[2 * g + 1];
   const int c1 = j.wctb[((size_t)s * j.NR + r1) * j.NB + b], c2 = j.wctb[((size_t)s * j.NR + r2) * j.NB + b];
   const size_t wpc = (size_t)j.half * j.NR, wpp = wpc * j.NB;
@@ -373,9 +385,14 @@ __global__ void k_hou_overlap(JobDev j, int g) {
 
 // Overlap bit of a site in natural order (x + L y + L^2 z): parity, half index
 // and bit of the multispin word (ini.c:355-375).
+void set_dividers(JobDev &j) {
+  j.fd_L.set(j.L); j.fd_S.set(j.L * j.L); j.fd_ml.set(j.msc_l); j.fd_mlz.set(j.msc_lz);
+  j.fd_hl.set(j.msc_l / 2); j.fd_nclust.set(j.nclust > 0 ? j.nclust : 1);
+}
+
 __device__ __forceinline__ int q_bit(const JobDev &j, const u64 *Q, int x, int y, int z) {
-  const int bx = x / j.msc_l, gx = x - bx * j.msc_l, by = y / j.msc_l, gy = y - by * j.msc_l;
-  const int bz = z / j.msc_lz, gz = z - bz * j.msc_lz;
+  const int bx = j.fd_ml.div(x), gx = x - bx * j.msc_l, by = j.fd_ml.div(y), gy = y - by * j.msc_l;
+  const int bz = j.fd_mlz.div(z), gz = z - bz * j.msc_lz;
   const int m = gx + j.msc_l * gy + j.msc_s * gz, p = (x ^ y ^ z) & 1;
   return (int)((Q[(size_t)p * j.half + (m >> 1)] >> (bx + 4 * by + 16 * bz)) & 1);
 }
@@ -439,13 +456,13 @@ __global__ void __launch_bounds__(512) k_cc_local(JobDev j, int D) {
   const int z0 = blockIdx.x * D, nz = min(D, j.Lz - z0), n = S * nz;
   const u64 *Q = j.Q + lat * 2 * j.half;
   for (int i = tid; i < n; i += nth) {
-    const int x = i % L, y = (i / L) % L, z = z0 + i / S;
-    qs[i] = (uint8_t)q_bit(j, Q, x, y, z);
+    const int zl = j.fd_S.div(i), xy = i - zl * S, y = j.fd_L.div(xy), x = xy - y * L;
+    qs[i] = (uint8_t)q_bit(j, Q, x, y, z0 + zl);
     lab[i] = (uint32_t)i;
   }
   __syncthreads();
   for (int i = tid; i < n; i += nth) {
-    const int x = i % L, y = (i / L) % L, zl = i / S, q = qs[i];
+    const int zl = j.fd_S.div(i), xy = i - zl * S, y = j.fd_L.div(xy), x = xy - y * L, q = qs[i];
     const int xm = x == 0 ? L - 1 : x - 1, ym = y == 0 ? L - 1 : y - 1;
     // site 0 tests its x-wrap bond against x = cc_xq (see JobDev::cc_xq)
     const int xt = (z0 == 0 && i == 0) ? j.cc_xq : xm;
@@ -463,11 +480,10 @@ __global__ void __launch_bounds__(512) k_cc_local(JobDev j, int D) {
 // merged into the global labels.
 __global__ void k_cc_merge(JobDev j, int D, int nslab) {
   const int L = j.L, S = L * L;
-  const size_t per_lat = (size_t)nslab * S;
-  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (size_t)j.ns * j.nclust * per_lat) return;
-  const size_t lat = t / per_lat;
-  const int r = (int)(t % per_lat), f = r / S, xy = r % S;
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nslab * S) return;
+  const size_t lat = blockIdx.y;
+  const int f = j.fd_S.div(r), xy = r - f * S;
   int z, zm;
   if (f == 0) {
     if (j.bc != EA_PBC) return;
@@ -475,7 +491,7 @@ __global__ void k_cc_merge(JobDev j, int D, int nslab) {
   } else {
     z = f * D; zm = z - 1;
   }
-  const int x = xy % L, y = xy / L;
+  const int y = j.fd_L.div(xy), x = xy - y * L;
   const u64 *Q = j.Q + lat * 2 * j.half;
   if (q_bit(j, Q, x, y, z) == q_bit(j, Q, x, y, zm))
     cc_unite(j.label + lat * j.V, (uint32_t)(xy + S * z), (uint32_t)(xy + S * zm));
@@ -513,28 +529,31 @@ __global__ void k_cc_flatten(JobDev j) {
 }
 
 // q' = q xor [U(root) < 0.5] packed back into words, then s_r1 ^= q', s_r2 ^= q'
-// (HoudayerXEA.cu:54-75,358-374; main.cu:776-832,938-991).
-__global__ void k_hou_apply(JobDev j, int g) {
-  const size_t n = (size_t)j.ns * j.nclust * 2 * j.half;
-  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const int k = (int)(i % j.half), p = (int)((i / j.half) & 1);
-  const size_t lat = i / (2 * (size_t)j.half);
-  const int b = (int)(lat % j.nclust), s = (int)(lat / j.nclust);
-  const uint32_t *lab = j.label + lat * j.V;
-  const double *U = j.U + ((size_t)s * j.NB + b) * j.V;
-  // coordinates of the word's MSC site
-  const int hl = j.msc_l >> 1;
-  const int row = k / hl, gy = row % j.msc_l, gz = row / j.msc_l;
-  const int gx = 2 * (k - row * hl) + ((gy + gz + p) & 1);
-  const int L = j.L, S = L * L;
-  u64 sel = 0;
-  for (int bit = 0; bit < 64; ++bit) {
+// (HoudayerXEA.cu:54-75,358-374; main.cu:776-832,938-991).  Two warps per
+// word, one lane per bit, so the 64 root lookups of a word run in parallel.
+__global__ void __launch_bounds__(256) k_hou_apply(JobDev j, int g) {
+  __shared__ unsigned s_sel[8];
+  const int t = threadIdx.x, wl = t >> 6, bit = t & 63;
+  const int w = blockIdx.x * 4 + wl;            // word of this lattice: parity * half + k
+  const size_t lat = blockIdx.y;
+  const size_t i = lat * 2 * j.half + w;
+  const bool valid = w < 2 * j.half;
+  const int p = w >= j.half, k = w - p * j.half;
+  const int s = j.fd_nclust.div((uint32_t)lat), b = (int)lat - s * j.nclust;
+  bool sel = false;
+  if (valid) {
+    const int hl = j.msc_l >> 1;
+    const int row = j.fd_hl.div(k), gz = j.fd_ml.div(row), gy = row - gz * j.msc_l;
+    const int gx = 2 * (k - row * hl) + ((gy + gz + p) & 1);
     const int x = gx + (bit & 3) * j.msc_l, y = gy + ((bit >> 2) & 3) * j.msc_l, z = gz + (bit >> 4) * j.msc_lz;
-    const uint32_t root = cc_find(lab, (uint32_t)(x + L * y + S * z));
-    sel |= (u64)(U[root] < 0.5) << bit;
+    const uint32_t root = cc_find(j.label + lat * j.V, (uint32_t)(x + j.L * y + j.L * j.L * z));
+    sel = __ldg(j.U + ((size_t)s * j.NB + b) * j.V + root) < 0.5;
   }
-  const u64 qn = j.Q[i] ^ sel;
+  const unsigned ball = __ballot_sync(0xffffffffu, sel);
+  if ((t & 31) == 0) s_sel[t >> 5] = ball;
+  __syncthreads();
+  if (!valid || bit != 0) return;
+  const u64 qn = j.Q[i] ^ ((u64)s_sel[2 * wl] | ((u64)s_sel[2 * wl + 1] << 32));
   const int r1 = j.pairs[2 * g], r2 = j.pairs[2 * g + 1];
   const int c1 = j.wctb[((size_t)s * j.NR + r1) * j.NB + b], c2 = j.wctb[((size_t)s * j.NR + r2) * j.NB + b];
   const size_t wpc = (size_t)j.half * j.NR, wpp = wpc * j.NB;
@@ -561,9 +580,9 @@ static cudaError_t launch_sweep_t(const JobDev &j, int parity, bool energy, bool
       cudaFuncSetAttribute(k_sweep<NR, KT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
       attr = true;
     }
-    k_sweep<NR, KT, true><<<j.ntiles, 256, sm, st>>>(j, parity, energy ? 1 : 0);
+    k_sweep<NR, KT, true><<<j.ntiles, 512, sm, st>>>(j, parity, energy ? 1 : 0);
   } else {
-    k_sweep<NR, KT, false><<<j.ntiles, 256, (size_t)KT * 8 * 4, st>>>(j, parity, 1);
+    k_sweep<NR, KT, false><<<j.ntiles, 512, (size_t)KT * 8 * 4, st>>>(j, parity, 1);
   }
   return cudaGetLastError();
 }
@@ -623,20 +642,20 @@ cudaError_t launch_houdayer_group(const JobDev &j, int g, cudaStream_t st) {
   const size_t nw = (size_t)j.ns * j.nclust * 2 * j.half;
   const size_t ns = (size_t)j.ns * j.nclust * j.V;
   const unsigned bw = (unsigned)((nw + 255) / 256), bs = (unsigned)((ns + 255) / 256);
-  k_hou_overlap<<<bw, 256, 0, st>>>(j, g);
+  const unsigned nlat = (unsigned)(j.ns * j.nclust);
+  k_hou_overlap<<<dim3((2 * j.half + 255) / 256, nlat), 256, 0, st>>>(j, g);
   const int S = j.L * j.L;
   if (S <= kSlabSites) {
     const int D = min(j.Lz, kSlabSites / S), nslab = (j.Lz + D - 1) / D;
     k_cc_local<<<dim3(nslab, j.ns * j.nclust), 512, 0, st>>>(j, D);
-    const size_t nm = (size_t)j.ns * j.nclust * nslab * S;
-    k_cc_merge<<<(unsigned)((nm + 255) / 256), 256, 0, st>>>(j, D, nslab);
+    k_cc_merge<<<dim3((nslab * S + 255) / 256, nlat), 256, 0, st>>>(j, D, nslab);
   } else {
     // planes too large for SMEM: Komura's passes on global labels
     k_cc_init<<<bs, 256, 0, st>>>(j);
     k_cc_flatten<<<bs, 256, 0, st>>>(j);
     k_cc_union<<<bs, 256, 0, st>>>(j);
   }
-  k_hou_apply<<<bw, 256, 0, st>>>(j, g);
+  k_hou_apply<<<dim3((2 * j.half + 3) / 4, nlat), 256, 0, st>>>(j, g);
   return cudaGetLastError();
 }
 

@@ -6,6 +6,28 @@
 
 namespace eagb {
 
+// Division by a value fixed at set-up, exact for every 32-bit numerator: one
+// multiply-high, an add and two shifts (the round-up method for unsigned
+// division by invariant integers, Granlund & Montgomery, PLDI 1994).
+struct FastDiv {
+  uint32_t d = 1, m = 1, s1 = 0, s2 = 0;
+  void set(uint32_t dd) {
+    d = dd ? dd : 1;
+    int l = 0;
+    while ((1ull << l) < d) ++l;
+    m = (uint32_t)((((1ull << 32) * ((1ull << l) - d)) / d) + 1);
+    s1 = l < 1 ? l : 1;
+    s2 = l > 1 ? l - 1 : 0;
+  }
+#ifdef __CUDACC__
+  __device__ __forceinline__ uint32_t div(uint32_t n) const {
+    const uint32_t t = __umulhi(m, n);
+    return (t + ((n - t) >> s1)) >> s2;
+  }
+  __device__ __forceinline__ uint32_t mod(uint32_t n) const { return n - div(n) * d; }
+#endif
+};
+
 // Everything a kernel needs about one job, by value (kernel parameter).
 // All arrays live in device memory, in the reference's layouts.
 struct JobDev {
@@ -49,7 +71,12 @@ struct JobDev {
   // i.e. (2^32-1+L) mod L, which differs from L-1 unless L is a power of two;
   // the union itself still joins sites 0 and L-1 (HoudayerXEA.cu:288).
   int cc_xq;
+  // dividers of the site <-> multispin-word maps
+  FastDiv fd_L, fd_S, fd_ml, fd_mlz, fd_hl, fd_nclust;
 };
+
+// Fills the dividers of j from its sizes (nclust included).
+void set_dividers(JobDev &j);
 
 // Tile width (half-sites per CTA) of the fused sweep kernel.
 int sweep_kt(const JobDev &j);

@@ -111,6 +111,7 @@ extern "C" int ea_measure_energy_noalloc(const ea_geom *gp, const uint64_t *d_sp
   j.NB = g.NB; j.NR = g.NR; j.ns = g.ns; j.half = g.half; j.msc_l = g.msc_l; j.msc_s = g.msc_s;
   j.msc_lz = g.msc_lz; j.L = g.L; j.Lz = g.Lz; j.V = g.V; j.bc = g.bc;
   j.kt = kt; j.ntiles = ntiles;
+  set_dividers(j);
   j.spins = const_cast<unsigned long long *>(reinterpret_cast<const unsigned long long *>(d_spins));
   j.J = reinterpret_cast<const unsigned long long *>(d_couplings);
   j.epart = reinterpret_cast<int32_t *>(base);

@@ -218,6 +218,14 @@ class Job:
         return avg, hist[:self.g.nsamples * self.g.nrep * m * self.g.nbetas].reshape(
             self.g.nsamples, self.g.nrep, m, self.g.nbetas)
 
+    def run_cycles(self, itmax, houfr, mesfr, ptfr, cluster=True, nclust=0):
+        """Enqueue one bin without copying anything back (asynchronous)."""
+        cad = Cadence(itmax, houfr, mesfr, ptfr, int(cluster), nclust)
+        _ck(lib().ea_run_bin(self.ctx, C.byref(cad), None, None, None))
+
+    def check_exact(self):
+        _ck(lib().ea_check_exact(self.ctx))
+
     def sync(self):
         _ck(lib().ea_sync(self.ctx))
 

@@ -185,11 +185,15 @@ int ea_set_cluster_rule(ea_ctx *ctx, int32_t rule);
  * avgE [nsamples][NR][NB] (sum over it, beta order) and hist [nsamples][NR][maxit][NB]
  * may be NULL; maxit_trw = itmax / frecTRW (io.c:431-434). */
 int ea_run_bin(ea_ctx *ctx, const ea_cadence *cad, double *avgE, uint8_t *hist, int32_t *maxit_trw);
+/* With avgE and hist both NULL, ea_run_bin only enqueues the bin and returns
+ * without synchronising; ea_check_exact then synchronises and reports
+ * EA_ERR_INEXACT if any tempering decision fell outside the exact exp table. */
+int ea_check_exact(ea_ctx *ctx);
 
 /* Per-kernel timing: while enabled, every launch of the listed kernels is
  * bracketed by CUDA events on the context's stream.  ea_kernel_time syncs and
  * returns the number of launches and their summed duration since enabling. */
-enum { EA_K_SWEEP = 0, EA_K_PT = 1, EA_K_CLUSTER = 2, EA_K_ENERGY = 3, EA_K_COUNT = 4 };
+enum { EA_K_SWEEP = 0, EA_K_PT = 1, EA_K_CLUSTER = 2, EA_K_ENERGY = 3, EA_K_RNG = 4, EA_K_COUNT = 5 };
 int ea_profile(ea_ctx *ctx, int32_t on);
 int ea_kernel_time(ea_ctx *ctx, int32_t kind, int64_t *launches, double *total_ms);
 
