@@ -165,28 +165,38 @@ def run_ours(args, rank, world, local):
     for _ in range(args.warmup):
         step()
     job.sync()
-    # timed region: device events on the job's stream, L2 flushed between steps
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    # timed region: device events on the job's stream around all K steps,
+    # joined with the generator stream at the end so that every uniform drawn
+    # inside the region is counted; the L2 flushes between steps are timed
+    # by their own events and taken out
+    t_beg, t_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    fl = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     barrier()
     torch.cuda.synchronize(dev)
     eagb._ck(eagb.lib().ea_profile(job.ctx, 1))
     with Clocks(dev) as clk, torch.cuda.stream(stream):
         for i in range(args.steps):
+            fl[i][0].record(stream)
             flush.fill_(i)
-            ev[i][0].record(stream)
+            fl[i][1].record(stream)
+            if i == 0:
+                t_beg.record(stream)
             step()
-            ev[i][1].record(stream)
+        job.join()
+        t_end.record(stream)
         job.sync()
     torch.cuda.synchronize(dev)
     job.check_exact()
     barrier()
-    ms = sum(a.elapsed_time(b) for a, b in ev)
+    ms = t_beg.elapsed_time(t_end) - sum(a.elapsed_time(b) for a, b in fl[1:])
     nsw, sw_ms = C.c_int64(), C.c_double()
     eagb._ck(eagb.lib().ea_kernel_time(job.ctx, 0, C.byref(nsw), C.byref(sw_ms)))
     npt, pt_ms = C.c_int64(), C.c_double()
     eagb._ck(eagb.lib().ea_kernel_time(job.ctx, 1, C.byref(npt), C.byref(pt_ms)))
     ncl, cl_ms = C.c_int64(), C.c_double()
     eagb._ck(eagb.lib().ea_kernel_time(job.ctx, 2, C.byref(ncl), C.byref(cl_ms)))
+    nrg, rg_ms = C.c_int64(), C.c_double()
+    eagb._ck(eagb.lib().ea_kernel_time(job.ctx, 4, C.byref(nrg), C.byref(rg_ms)))
     eagb._ck(eagb.lib().ea_profile(job.ctx, 0))
 
     # end to end through the C ABI with host buffers: every step uploads the
@@ -238,14 +248,16 @@ def run_ours(args, rank, world, local):
         "data": "synthetic (seeded couplings and spins as the reference generates them)",
         "config": {"workload": WORKLOAD, "L": L, "Lz": LZ, "nbetas": NB, "nrep": NR, "nsamples": NS,
                    "bc": "OBC", "ptfr": 1, "houfr": HOUFR, "form": "plain (one job per launch)",
-                   "l2": "flushed between steps (512 MB write)", "parallelism": "replicas" if world > 1 else "single"},
+                   "l2": "flushed between steps (512 MB write)", "parallelism": "replicas" if world > 1 else "single",
+                   "rng_sms": job.rng_sms()},
         "e2e": {"value": e2e, "unit": "spin-updates/ps", "h2d_bytes_per_step": NS * 2 * nw * 8,
                 "d2h_bytes_per_step": NS * NR * NB * 4},
         "gpu_launches": args.steps * (HOUFR * 6 + 1 + 2 * 4 + 3),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": None, "kernel": "k_sweep", "peak_kind": how,
                      "alg_bytes_per_launch": alg_bytes, "launch_ms": sweep_ms, "launches": nsw.value},
-        "kernel_ms": {"sweep": sw_ms.value, "pt": pt_ms.value, "cluster": cl_ms.value, "step_total": ms},
+        "kernel_ms": {"sweep": sw_ms.value, "pt": pt_ms.value, "cluster": cl_ms.value,
+                      "uniforms_overlapped": rg_ms.value, "step_total": ms},
         "clocks": clk.summary(),
     }
     if not args.no_cpu:

@@ -1,9 +1,10 @@
 // api.cu -- the C ABI of libeagb.so (declared in include/eagb.h).
 //
-// A context is one job: it owns every device buffer and one stream, and
-// enqueues the kernels of kernels.cu in the order of the reference driver
-// (PROGRAM/src/main.cu:142-230).  No call synchronises the device except the
-// ones that return data to the host.
+// A context is one job: it owns every device buffer and two streams (the job's
+// and the cluster-uniform generator's), and enqueues the kernels of kernels.cu
+// in the order of the reference driver (PROGRAM/src/main.cu:142-230).  No call
+// synchronises the device except the ones that return data to the host.
+#include <cuda.h>
 #include <curand.h>
 
 #include <cmath>
@@ -62,11 +63,21 @@ struct ea_ctx {
   curandGenerator_t gen = nullptr;
   uint64_t cuda_rng_offset = 0, seed_cluster = 0;
   int nclust_cap = 0;
-  // uniforms of the two groups of a move.  They are drawn on the job's own
-  // stream: drawn on a second stream overlapping the sweeps, the generator ran
-  // about 4x slower once moves were queued back to back.
-  double *U[2] = {nullptr, nullptr};
-  bool pregen = false;
+  // Uniforms of a move: U[set][group].  The generator runs on its own stream
+  // `rs` at the highest priority and draws the next move's set while the
+  // current move and the sweeps after it run on `st`.  Its kernel holds 64
+  // blocks of 64 threads and is bound by FP64 throughput on the SMs it
+  // holds, so it overlaps the integer kernels of the job almost entirely.
+  // The sequence of uniforms is the generator's own, whatever the overlap.
+  cudaStream_t rs = nullptr;
+  // optional SM partition (green contexts): the generator on its own SMs,
+  // the job's kernels on the rest
+  CUgreenCtx part[2] = {nullptr, nullptr};
+  int part_sms = 0;
+  double *U[2][2] = {};
+  cudaEvent_t drawn[2] = {}, used[2] = {};
+  int cur = 0;    // set that holds the uniforms of the next move
+  int ready = 0;  // sets drawn and not yet used by a move (0..2)
   uint32_t *label = nullptr;
   unsigned long long *Q = nullptr;
   // measurement buffers
@@ -143,6 +154,59 @@ static void prof_collect(ea_ctx *c) {
     }
     c->prof_ev[k].clear();
   }
+}
+
+
+// Driver entry points of the green-context API, looked up at run time so
+// that the library needs no link to the driver library.
+static void *drv_fn(const char *name) {
+  void *fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion(name, &fn, CUDA_VERSION, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess)
+    return nullptr;
+  return fn;
+}
+
+// Splits the device into nsm SMs for the cluster-uniform generator and the
+// rest for the job, and creates the two streams there.
+static int make_partition(ea_ctx *c, int nsm) {
+  using GetRes = CUresult (*)(CUdevice, CUdevResource *, CUdevResourceType);
+  using Split = CUresult (*)(CUdevResource *, unsigned *, const CUdevResource *, CUdevResource *, unsigned, unsigned);
+  using GenDesc = CUresult (*)(CUdevResourceDesc *, CUdevResource *, unsigned);
+  using GCreate = CUresult (*)(CUgreenCtx *, CUdevResourceDesc, CUdevice, unsigned);
+  using GStream = CUresult (*)(CUstream *, CUgreenCtx, unsigned, int);
+  using DevGet = CUresult (*)(CUdevice *, int);
+  auto devget = (DevGet)drv_fn("cuDeviceGet");
+  auto getres = (GetRes)drv_fn("cuDeviceGetDevResource");
+  auto split = (Split)drv_fn("cuDevSmResourceSplitByCount");
+  auto gendesc = (GenDesc)drv_fn("cuDevResourceGenerateDesc");
+  auto gcreate = (GCreate)drv_fn("cuGreenCtxCreate");
+  auto gstream = (GStream)drv_fn("cuGreenCtxStreamCreate");
+  if (!devget || !getres || !split || !gendesc || !gcreate || !gstream)
+    return fail(EA_ERR_CUDA, "green contexts are not available from this driver");
+  CUdevice dev;
+  CUdevResource all, grp, rest;
+  unsigned ng = 1;
+  CUdevResourceDesc d[2];
+  CUstream s[2];
+  if (devget(&dev, c->device) || getres(dev, &all, CU_DEV_RESOURCE_TYPE_SM) ||
+      split(&grp, &ng, &all, &rest, 0, (unsigned)nsm) || ng != 1 || gendesc(&d[0], &grp, 1) ||
+      gendesc(&d[1], &rest, 1) || gcreate(&c->part[0], d[0], dev, CU_GREEN_CTX_DEFAULT_STREAM) ||
+      gcreate(&c->part[1], d[1], dev, CU_GREEN_CTX_DEFAULT_STREAM) ||
+      gstream(&s[0], c->part[0], CU_STREAM_NON_BLOCKING, 0) || gstream(&s[1], c->part[1], CU_STREAM_NON_BLOCKING, 0))
+    return fail(EA_ERR_CUDA, "SM partition of %d SMs failed", nsm);
+  c->rs = (cudaStream_t)s[0];
+  c->st = (cudaStream_t)s[1];
+  c->part_sms = (int)grp.sm.smCount;
+  return EA_OK;
+}
+
+static void drop_partition(ea_ctx *c) {
+  using GDestroy = CUresult (*)(CUgreenCtx);
+  auto gdestroy = (GDestroy)drv_fn("cuGreenCtxDestroy");
+  for (CUgreenCtx &g : c->part)
+    if (g && gdestroy) { gdestroy(g); g = nullptr; }
 }
 
 
@@ -311,7 +375,53 @@ int ea_create(const ea_geom *gp, int32_t device, ea_ctx **out) {
   CU(cudaMemcpyAsync((void *)j.nbflag, fl.data(), fl.size(), cudaMemcpyHostToDevice, c->st));
   if ((rc = ea_set_permutations(c, nullptr)) != EA_OK) { ea_destroy(c); return rc; }
   CU(cudaStreamSynchronize(c->st));
+  if ((rc = ea_set_rng_sms(c, -1)) != EA_OK) { ea_destroy(c); return rc; }
   *out = c;
+  return EA_OK;
+}
+
+int ea_get_rng_sms(const ea_ctx *c, int32_t *nsm) {
+  if (!c || !nsm) return fail(EA_ERR_ARG, "null argument");
+  *nsm = c->part_sms;
+  return EA_OK;
+}
+
+int ea_set_rng_sms(ea_ctx *c, int32_t nsm) {
+  if (check(c)) return EA_ERR_ARG;
+  if (c->gen) return fail(EA_ERR_STATE, "the SM split is set before the first cluster move");
+  if (set_device(c)) return EA_ERR_CUDA;
+  const Geometry &g = c->g;
+  int nsms = 0;
+  CU(cudaDeviceGetAttribute(&nsms, cudaDevAttrMultiProcessorCount, c->device));
+  if (nsm < 0) nsm = (2.0 * g.V * g.NB * g.ns >= (double)(1 << 24) && nsms >= 128) ? 32 : 0;
+  if (nsm >= nsms) return fail(EA_ERR_ARG, "SM split %d of %d SMs", nsm, nsms);
+  if (nsm == c->part_sms) return EA_OK;
+  CU(cudaStreamSynchronize(c->st));
+  if (c->rs) CU(cudaStreamSynchronize(c->rs));
+  cudaStream_t old_st = c->st, old_rs = c->rs;
+  CUgreenCtx old_part[2] = {c->part[0], c->part[1]};
+  c->part[0] = c->part[1] = nullptr;
+  c->rs = nullptr;
+  int rc = EA_OK;
+  if (nsm > 0) {
+    rc = make_partition(c, nsm);
+  } else {
+    cudaError_t e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) rc = fail(EA_ERR_CUDA, "stream: %s", cudaGetErrorString(e));
+    c->part_sms = 0;
+  }
+  if (rc != EA_OK) {
+    drop_partition(c);
+    c->st = old_st; c->rs = old_rs;
+    c->part[0] = old_part[0]; c->part[1] = old_part[1];
+    return rc;
+  }
+  if (old_rs) cudaStreamDestroy(old_rs);
+  cudaStreamDestroy(old_st);
+  using GDestroy = CUresult (*)(CUgreenCtx);
+  auto gdestroy = (GDestroy)drv_fn("cuGreenCtxDestroy");
+  for (CUgreenCtx gx : old_part)
+    if (gx && gdestroy) gdestroy(gx);
   return EA_OK;
 }
 
@@ -319,16 +429,25 @@ int ea_destroy(ea_ctx *c) {
   if (!c) return EA_OK;
   cudaSetDevice(c->device);
   if (c->st) cudaStreamSynchronize(c->st);
+  if (c->rs) cudaStreamSynchronize(c->rs);
   if (c->gen) curandDestroyGenerator(c->gen);
   prof_collect(c);
   for (void *p : c->owned) cudaFree(p);
-  for (double *u : c->U)
-    if (u) cudaFree(u);
+  for (auto &set : c->U)
+    for (double *u : set)
+      if (u) cudaFree(u);
+  for (int s = 0; s < 2; ++s) {
+    if (c->drawn[s]) cudaEventDestroy(c->drawn[s]);
+    if (c->used[s]) cudaEventDestroy(c->used[s]);
+  }
+  if (c->rs) cudaStreamDestroy(c->rs);
+  if (c->st) cudaStreamDestroy(c->st);
+  c->st = nullptr;
+  drop_partition(c);
   if (c->label) cudaFree(c->label);
   if (c->Q) cudaFree(c->Q);
   if (c->hist) cudaFree(c->hist);
   if (c->exptab) cudaFree(c->exptab);
-  if (c->st) cudaStreamDestroy(c->st);
   delete c;
   return EA_OK;
 }
@@ -342,6 +461,19 @@ int ea_get_geom(const ea_ctx *c, ea_geom *g) {
 int ea_sync(ea_ctx *c) {
   if (check(c)) return EA_ERR_ARG;
   CU(cudaStreamSynchronize(c->st));
+  if (c->rs) CU(cudaStreamSynchronize(c->rs));
+  return EA_OK;
+}
+
+int ea_join(ea_ctx *c) {
+  if (check(c)) return EA_ERR_ARG;
+  if (!c->rs) return EA_OK;
+  if (set_device(c)) return EA_ERR_CUDA;
+  cudaEvent_t e;
+  CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  CU(cudaEventRecord(e, c->rs));
+  CU(cudaStreamWaitEvent(c->st, e, 0));
+  CU(cudaEventDestroy(e));
   return EA_OK;
 }
 
@@ -422,15 +554,15 @@ int ea_set_generators(ea_ctx *c, const ea_generators *gen, const ea_hq *pt) {
   CU(cudaMemcpyAsync(c->j.rc, &gen->rc, sizeof(ea_hq), cudaMemcpyHostToDevice, c->st));
   CU(cudaMemcpyAsync(c->j.pt, pt, sizeof(ea_hq) * g.ns * g.NR, cudaMemcpyHostToDevice, c->st));
   CU(cudaStreamSynchronize(c->st));
-  if (c->pregen) {
-    // uniforms drawn ahead for a move that has not run are given back
-    c->cuda_rng_offset -= 2 * (uint64_t)g.V * g.NB * g.ns;
-    c->pregen = false;
-    if (c->gen) { curandDestroyGenerator(c->gen); c->gen = nullptr; }
-  }
+  // The same cluster seed and offset as the job's own continue its generator
+  // (uniforms drawn ahead included), as the reference process keeps its
+  // generator across bins; other values start a new generator there, as
+  // ClusterInit does on a restart.
   if (c->gen && (gen->seed_cluster != c->seed_cluster || gen->cuda_rng_offset != c->cuda_rng_offset)) {
+    CU(cudaStreamSynchronize(c->rs));
     curandDestroyGenerator(c->gen);
     c->gen = nullptr;
+    c->ready = 0;
   }
   c->cuda_rng_offset = gen->cuda_rng_offset;
   c->seed_cluster = gen->seed_cluster;
@@ -605,8 +737,20 @@ int ea_parallel_tempering(ea_ctx *c) {
 
 static int ensure_cluster(ea_ctx *c, int nclust) {
   const Geometry &g = c->g;
-  for (double *&u : c->U)
-    if (!u) CU(dalloc(u, (size_t)g.V * g.NB * g.ns));
+  if (!c->rs) {
+    int least = 0, greatest = 0;
+    CU(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    CU(cudaStreamCreateWithPriority(&c->rs, cudaStreamNonBlocking, greatest));
+  }
+  if (!c->drawn[0]) {
+    for (int s = 0; s < 2; ++s) {
+      CU(cudaEventCreateWithFlags(&c->drawn[s], cudaEventDisableTiming));
+      CU(cudaEventCreateWithFlags(&c->used[s], cudaEventDisableTiming));
+    }
+  }
+  for (auto &set : c->U)
+    for (double *&u : set)
+      if (!u) CU(dalloc(u, (size_t)g.V * g.NB * g.ns));
   if (nclust > c->nclust_cap) {
     CU(cudaStreamSynchronize(c->st));
     if (c->label) cudaFree(c->label);
@@ -626,7 +770,8 @@ static int ensure_cluster(ea_ctx *c, int nclust) {
     CR(curandCreateGenerator(&c->gen, CURAND_RNG_PSEUDO_DEFAULT));
     CR(curandSetPseudoRandomGeneratorSeed(c->gen, (unsigned long long)c->seed_cluster));
     if (c->cuda_rng_offset > 0) CR(curandSetGeneratorOffset(c->gen, c->cuda_rng_offset));
-    CR(curandSetStream(c->gen, c->st));
+    CR(curandSetStream(c->gen, c->rs));
+    c->ready = 0;
   }
   return EA_OK;
 }
@@ -636,21 +781,17 @@ static int norm_nclust(const Geometry &g, int nclust) {
   return nclust > g.NB ? g.NB : nclust;
 }
 
-// ClusterStep's uniforms (HoudayerXEA.cu:189-195) for both groups of a move:
-// V*NB*nsamples doubles per group, in the reference's call sizes.
-static int houdayer_generate(ea_ctx *c, int nclust) {
+// ClusterStep's uniforms (HoudayerXEA.cu:189-195) for both groups of one move,
+// V*NB*nsamples doubles per group in the reference's call sizes, into set
+// `set` once the move that last read it has finished.
+static int houdayer_draw(ea_ctx *c, int set) {
   const Geometry &g = c->g;
-  if (c->pregen) return EA_OK;
-  int rc = ensure_cluster(c, norm_nclust(g, nclust));
-  if (rc) return rc;
   const size_t tot = (size_t)g.V * g.NB * g.ns;
-  cudaEvent_t b = prof_begin(c);
-  for (int grp = 0; grp < 2; ++grp) {
-    CR(curandGenerateUniformDouble(c->gen, c->U[grp], tot));
-    c->cuda_rng_offset += tot;
-  }
-  prof_end(c, EA_K_RNG, b);
-  c->pregen = true;
+  CU(cudaStreamWaitEvent(c->rs, c->used[set], 0));
+  cudaEvent_t b = prof_begin(c, c->rs);
+  for (int grp = 0; grp < 2; ++grp) CR(curandGenerateUniformDouble(c->gen, c->U[set][grp], tot));
+  prof_end(c, EA_K_RNG, b, c->rs);
+  CU(cudaEventRecord(c->drawn[set], c->rs));
   return EA_OK;
 }
 
@@ -658,19 +799,30 @@ static int houdayer(ea_ctx *c, int nclust) {
   const Geometry &g = c->g;
   if (g.NR < 4) return fail(EA_ERR_ARG, "the Houdayer move needs at least 2 replicas per group");
   nclust = norm_nclust(g, nclust);
-  int rc = houdayer_generate(c, nclust);
+  int rc = ensure_cluster(c, nclust);
   if (rc) return rc;
-  rc = ensure_cluster(c, nclust);
-  if (rc) return rc;
+  if (c->ready == 0) {
+    if ((rc = houdayer_draw(c, c->cur))) return rc;
+    c->ready = 1;
+  }
+  // the next move's uniforms, drawn while this move and the sweeps after it run
+  if (c->ready == 1) {
+    if ((rc = houdayer_draw(c, c->cur ^ 1))) return rc;
+    c->ready = 2;
+  }
   CU(launch_houdayer_pairs(c->j, c->st));
+  CU(cudaStreamWaitEvent(c->st, c->drawn[c->cur], 0));
   for (int grp = 0; grp < 2; ++grp) {
     JobDev jg = c->j;
-    jg.U = c->U[grp];
+    jg.U = c->U[c->cur][grp];
     cudaEvent_t b = prof_begin(c);
     CU(launch_houdayer_group(jg, grp, c->st));
     prof_end(c, EA_K_CLUSTER, b);
   }
-  c->pregen = false;
+  CU(cudaEventRecord(c->used[c->cur], c->st));
+  c->cur ^= 1;
+  c->ready = 1;
+  c->cuda_rng_offset += 2 * (uint64_t)g.V * g.NB * g.ns;
   c->energies_fresh = false;
   return EA_OK;
 }

@@ -715,6 +715,8 @@ int main(int argc, char **argv) {
   // device job
   ea_ctx *ctx = nullptr;
   ck(ea_create(&geo, device, &ctx), "ea_create");
+  // without cluster moves no uniforms are drawn: the job keeps every SM
+  if (!bld.cluster) ck(ea_set_rng_sms(ctx, 0), "SM split");
   ck(ea_set_temperatures(ctx, betas.data(), cum.data()), "temperatures");
   gen.seed_cluster = data.seed_C;
   ck(ea_set_generators(ctx, &gen, pt.data()), "generators");

@@ -448,6 +448,96 @@ __device__ __forceinline__ void cc_unite(uint32_t *lab, uint32_t a, uint32_t b) 
 // slab piece; only bonds between slabs are left for k_cc_merge.
 constexpr int kSlabSites = 8192;
 
+// Planes of up to 1024 sites: one thread per (x, y) column and P planes
+// (at most 16 sites a thread), in lock-step rounds so that no lane walks a
+// long chain while the others wait:
+//   hook:  every bond whose two labels differ hangs the larger label below
+//          the smaller (atomicMin);
+//   jump:  lab[i] = lab[lab[i]] until every label is a root;
+// until a hook round finds nothing to do.  Labels only decrease and always
+// name a site of the same cluster, so at the end every site holds the
+// smallest index of its slab cluster.  The bonds are those of the union-find
+// of the reference (HoudayerXEA.cu:77-121): -x and -y periodic, -z inside the
+// slab.
+constexpr int kSlabMaxPerThread = 16;
+
+__global__ void __launch_bounds__(1024) k_cc_slab(JobDev j, int D, int P) {
+  __shared__ uint32_t lab[kSlabSites];
+  __shared__ uint8_t qs[kSlabSites];
+  const int L = j.L, S = L * L, t = threadIdx.x;
+  const size_t lat = blockIdx.y;
+  const int z0 = blockIdx.x * D, nz = min(D, j.Lz - z0);
+  const u64 *Q = j.Q + lat * 2 * j.half;
+  const int zp = j.fd_S.div(t), xy = t - zp * S, y = j.fd_L.div(xy), x = xy - y * L;
+  {
+    const int bx = j.fd_ml.div(x), by = j.fd_ml.div(y);
+    const int mxy = (x - bx * j.msc_l) + j.msc_l * (y - by * j.msc_l), sxy = bx + 4 * by;
+    int z = z0 + zp, bz = j.fd_mlz.div(z), gz = z - bz * j.msc_lz;
+    for (int zl = zp; zl < nz; zl += P) {
+      const int i = xy + S * zl, m = mxy + j.msc_s * gz, p = (x ^ y ^ z) & 1;
+      qs[i] = (uint8_t)((Q[(size_t)p * j.half + (m >> 1)] >> (sxy + 16 * bz)) & 1);
+      lab[i] = (uint32_t)i;
+      z += P;
+      gz += P;
+      while (gz >= j.msc_lz) { gz -= j.msc_lz; ++bz; }
+    }
+  }
+  __syncthreads();
+  const int xm = x == 0 ? L - 1 : x - 1, ym = y == 0 ? L - 1 : y - 1;
+  const int ixm = xm + L * y, iym = x + L * ym;
+  // bond bits of this thread's sites: 3 per site (-x, -y, -z)
+  u64 bonds = 0;
+  {
+    int k = 0;
+    for (int zl = zp; zl < nz; zl += P, ++k) {
+      const int i = xy + S * zl, q = qs[i], pl = S * zl;
+      // site 0 tests its x-wrap bond against x = cc_xq (see JobDev::cc_xq)
+      const int xt = (z0 == 0 && i == 0) ? j.cc_xq : xm;
+      const u64 b = (u64)(qs[xt + L * y + pl] == q) | ((u64)(qs[iym + pl] == q) << 1) |
+                    ((u64)(zl > 0 && qs[i - S] == q) << 2);
+      bonds |= b << (3 * k);
+    }
+  }
+  for (;;) {
+    int hooked = 0;
+    {
+      int k = 0;
+      for (int zl = zp; zl < nz; zl += P, ++k) {
+        const unsigned b = (unsigned)(bonds >> (3 * k)) & 7u;
+        if (!b) continue;
+        const int i = xy + S * zl, pl = S * zl;
+        const uint32_t li = lab[i];
+        if (b & 1) {
+          const uint32_t lj = lab[ixm + pl];
+          if (lj != li) { atomicMin(&lab[max(li, lj)], min(li, lj)); hooked = 1; }
+        }
+        if (b & 2) {
+          const uint32_t lj = lab[iym + pl];
+          if (lj != li) { atomicMin(&lab[max(li, lj)], min(li, lj)); hooked = 1; }
+        }
+        if (b & 4) {
+          const uint32_t lj = lab[i - S];
+          if (lj != li) { atomicMin(&lab[max(li, lj)], min(li, lj)); hooked = 1; }
+        }
+      }
+    }
+    if (!__syncthreads_or(hooked)) break;
+    for (;;) {
+      int moved = 0;
+      for (int zl = zp; zl < nz; zl += P) {
+        const int i = xy + S * zl;
+        const uint32_t l = lab[i], ll = lab[l];
+        if (ll != l) { lab[i] = ll; moved = 1; }
+      }
+      if (!__syncthreads_or(moved)) break;
+    }
+  }
+  uint32_t *glab = j.label + lat * j.V + (size_t)z0 * S;
+  const uint32_t off = (uint32_t)z0 * S;
+  for (int zl = zp; zl < nz; zl += P) glab[xy + S * zl] = off + lab[xy + S * zl];
+}
+
+// Planes of 1025..8192 sites: a CTA-wide loop over the slab's sites.
 __global__ void __launch_bounds__(512) k_cc_local(JobDev j, int D) {
   __shared__ uint32_t lab[kSlabSites];
   __shared__ uint8_t qs[kSlabSites];
@@ -647,7 +737,12 @@ cudaError_t launch_houdayer_group(const JobDev &j, int g, cudaStream_t st) {
   const int S = j.L * j.L;
   if (S <= kSlabSites) {
     const int D = min(j.Lz, kSlabSites / S), nslab = (j.Lz + D - 1) / D;
-    k_cc_local<<<dim3(nslab, j.ns * j.nclust), 512, 0, st>>>(j, D);
+    const int P = max(1, min(D, 512 / S));
+    if (S <= 1024 && (D + P - 1) / P <= kSlabMaxPerThread) {
+      k_cc_slab<<<dim3(nslab, j.ns * j.nclust), S * P, 0, st>>>(j, D, P);
+    } else {
+      k_cc_local<<<dim3(nslab, j.ns * j.nclust), 512, 0, st>>>(j, D);
+    }
     k_cc_merge<<<dim3((nslab * S + 255) / 256, nlat), 256, 0, st>>>(j, D, nslab);
   } else {
     // planes too large for SMEM: Komura's passes on global labels

@@ -229,6 +229,19 @@ class Job:
     def sync(self):
         _ck(lib().ea_sync(self.ctx))
 
+    def join(self):
+        _ck(lib().ea_join(self.ctx))
+
+    def set_rng_sms(self, nsm):
+        """SM split between the cluster-uniform generator and the job (0: none,
+        negative: automatic); before the first cluster move only."""
+        _ck(lib().ea_set_rng_sms(self.ctx, int(nsm)))
+
+    def rng_sms(self):
+        v = C.c_int32()
+        _ck(lib().ea_get_rng_sms(self.ctx, C.byref(v)))
+        return v.value
+
     def stream(self):
         v = C.c_void_p()
         _ck(lib().ea_get_stream(self.ctx, C.byref(v)))

@@ -117,10 +117,18 @@ typedef struct ea_ctx ea_ctx;
 int ea_create(const ea_geom *g, int32_t device, ea_ctx **out);
 int ea_destroy(ea_ctx *ctx);
 int ea_get_geom(const ea_ctx *ctx, ea_geom *g);
+/* Waits for all work of the context (its stream and its generator stream). */
 int ea_sync(ea_ctx *ctx);
 /* The context's CUDA stream (a cudaStream_t), so callers can order their own
- * work or timing events with the job's kernels. */
+ * work or timing events with the job's kernels.  The cluster uniforms of the
+ * next Houdayer move are drawn ahead on a second stream of the context. */
 int ea_get_stream(ea_ctx *ctx, void **stream);
+/* Makes the context's stream wait for the work queued so far on its
+ * generator stream (the uniforms drawn ahead), without a host
+ * synchronisation: an event recorded on the stream afterwards covers all
+ * work of the job.  No reference counterpart (the reference draws the
+ * uniforms inside the move, HoudayerXEA.cu:189-195). */
+int ea_join(ea_ctx *ctx);
 
 /* Inputs.  betas descending (read_betas, io.c:476-501); cum: [NB][256] (read_lut, io.c:504-534). */
 int ea_set_temperatures(ea_ctx *ctx, const double *betas, const uint64_t *cum);
@@ -180,6 +188,19 @@ int ea_houdayer(ea_ctx *ctx, int32_t nclust);
  * E(r1)+E(r2) for every L. */
 enum { EA_CLUSTER_REFERENCE = 0, EA_CLUSTER_EXACT = 1 };
 int ea_set_cluster_rule(ea_ctx *ctx, int32_t rule);
+/* SM split between the cluster-uniform generator and the job's kernels.
+ * cuRAND's XORWOW generator runs 64 blocks of 64 threads whose length is set
+ * by the call size; on its own green-context partition of nsm SMs it keeps
+ * its full speed (nsm >= 32) while the job's kernels run on the other SMs,
+ * and the two overlap.  nsm = 0: no partition (the generator runs on a
+ * high-priority stream over the whole device); nsm < 0: automatic, 32 SMs when
+ * a move draws at least 2^24 uniforms (ea_create applies it), else none.
+ * Allowed before the first cluster move only; it replaces the context's
+ * streams, so a handle from ea_get_stream taken earlier is stale.  No
+ * reference counterpart (results do not depend on it). */
+int ea_set_rng_sms(ea_ctx *ctx, int32_t nsm);
+/* SMs of the generator's partition (0: none). */
+int ea_get_rng_sms(const ea_ctx *ctx, int32_t *nsm);
 /* One bin (main.cu:149-230): itmax x mesfr x (houfr x (MC + energy + PT) + Houdayer),
  * then the per-it energy measure, average and temperature-history record.
  * avgE [nsamples][NR][NB] (sum over it, beta order) and hist [nsamples][NR][maxit][NB]

@@ -167,3 +167,39 @@ def test_large_tube_bin():
     assert np.array_equal(avg, sim.avgE)
     assert_same_state(job, sim)
     job.close()
+
+
+def test_uniforms_drawn_ahead_continue_across_calls():
+    """The next move's uniforms are drawn ahead on the generator stream: asynchronous
+    bins, a generator read-back and a re-upload of the same state in between must
+    leave the sequence as the reference process's single generator draws it."""
+    job, sim = make("L8_Lz16_OBC", jobid=9, iter0=0)
+    it = 0
+    job.run_cycles(itmax=2, houfr=1, mesfr=1, ptfr=1)
+    it = sim.run_bin(itmax=2, houfr=1, mesfr=1, ptfr=1, iter0=it, jobid=9)
+    gen, pt = job.get_generators()
+    assert gen.cuda_rng_offset == sim.cuda_rng_offset
+    job.set_generators(gen, pt)
+    avg, hist = job.run_bin(itmax=3, houfr=1, mesfr=2, ptfr=1, cluster=True)
+    it = sim.run_bin(itmax=3, houfr=1, mesfr=2, ptfr=1, iter0=it, jobid=9)
+    assert np.array_equal(avg, sim.avgE)
+    assert_same_state(job, sim)
+    gen, _ = job.get_generators()
+    assert gen.cuda_rng_offset == sim.cuda_rng_offset
+    job.close()
+
+
+@pytest.mark.parametrize("nsm", [0, 32, 48])
+def test_sm_split_leaves_results_unchanged(nsm):
+    """The generator's SM partition changes only where kernels run."""
+    betas, cum = lut("T06_16_N32")
+    job = eagb.new_job(24, 192, betas, cum, nsamples=2, bc=O.OBC, masters=MASTERS, iter0=0, jobid=4)
+    job.set_rng_sms(nsm)
+    sim = O.Sim(24, 192, betas, cum, nbits=2, bc=O.OBC, masters=MASTERS, itmax=2)
+    avg, hist = job.run_bin(itmax=2, houfr=1, mesfr=1, ptfr=1, cluster=True)
+    sim.run_bin(itmax=2, houfr=1, mesfr=1, ptfr=1, iter0=0, jobid=4)
+    assert np.array_equal(avg, sim.avgE)
+    assert_same_state(job, sim)
+    with pytest.raises(eagb.EAError):
+        job.set_rng_sms(16)      # only before the first cluster move
+    job.close()
