@@ -16,6 +16,7 @@
 
 #include "eagb.h"
 #include "host.hpp"
+#include "batch.cuh"
 #include "kernels.cuh"
 
 using namespace eagb;
@@ -795,21 +796,38 @@ static int houdayer_draw(ea_ctx *c, int set) {
   return EA_OK;
 }
 
-static int houdayer(ea_ctx *c, int nclust) {
+// Everything of a move that happens before its kernels: buffers, the
+// generator, and the uniforms of this move (and of the next one, drawn ahead).
+static int houdayer_prepare(ea_ctx *c, int nclust) {
   const Geometry &g = c->g;
   if (g.NR < 4) return fail(EA_ERR_ARG, "the Houdayer move needs at least 2 replicas per group");
-  nclust = norm_nclust(g, nclust);
-  int rc = ensure_cluster(c, nclust);
+  int rc = ensure_cluster(c, norm_nclust(g, nclust));
   if (rc) return rc;
   if (c->ready == 0) {
     if ((rc = houdayer_draw(c, c->cur))) return rc;
     c->ready = 1;
   }
-  // the next move's uniforms, drawn while this move and the sweeps after it run
   if (c->ready == 1) {
     if ((rc = houdayer_draw(c, c->cur ^ 1))) return rc;
     c->ready = 2;
   }
+  return EA_OK;
+}
+
+// After the move's kernels were enqueued on stream s.
+static int houdayer_finish(ea_ctx *c, cudaStream_t s) {
+  const Geometry &g = c->g;
+  CU(cudaEventRecord(c->used[c->cur], s));
+  c->cur ^= 1;
+  c->ready = 1;
+  c->cuda_rng_offset += 2 * (uint64_t)g.V * g.NB * g.ns;
+  c->energies_fresh = false;
+  return EA_OK;
+}
+
+static int houdayer(ea_ctx *c, int nclust) {
+  int rc = houdayer_prepare(c, nclust);
+  if (rc) return rc;
   CU(launch_houdayer_pairs(c->j, c->st));
   CU(cudaStreamWaitEvent(c->st, c->drawn[c->cur], 0));
   for (int grp = 0; grp < 2; ++grp) {
@@ -819,12 +837,7 @@ static int houdayer(ea_ctx *c, int nclust) {
     CU(launch_houdayer_group(jg, grp, c->st));
     prof_end(c, EA_K_CLUSTER, b);
   }
-  CU(cudaEventRecord(c->used[c->cur], c->st));
-  c->cur ^= 1;
-  c->ready = 1;
-  c->cuda_rng_offset += 2 * (uint64_t)g.V * g.NB * g.ns;
-  c->energies_fresh = false;
-  return EA_OK;
+  return houdayer_finish(c, c->st);
 }
 
 int ea_houdayer(ea_ctx *c, int32_t nclust) {
@@ -932,6 +945,306 @@ int ea_curand_uniforms(int32_t device, uint64_t seed, uint64_t offset, uint64_t 
   cudaFree(d);
   if (e != cudaSuccess) return fail(EA_ERR_CUDA, "%s", cudaGetErrorString(e));
   return EA_OK;
+}
+
+
+// ---------------------------------------------------------------------------
+// Batches: many jobs (geometries, boundary conditions, temperature counts)
+// advanced by persistent batched kernels, one launch per step for all of
+// them, with the sweep / energy / tempering cycle replayed as a CUDA graph.
+// ---------------------------------------------------------------------------
+}  // extern "C"
+
+struct ea_batch {
+  std::vector<ea_ctx *> jobs;
+  int device = 0, NR = 0, KT = 0, NBmax = 0;
+  cudaStream_t bs = nullptr;
+  cudaEvent_t done = nullptr;
+  JobDev *d_jobs = nullptr;
+  uint32_t *d_pre = nullptr;
+  std::vector<JobDev> up_jobs;  // JobDev array as last uploaded
+  std::vector<uint32_t> up_pre;
+  BatchDev bd{};
+  cudaGraphExec_t cycle = nullptr;
+  int cycle_ptfr = -1;
+  UTable u{};  // uniforms of the current group, by job
+};
+
+extern "C" {
+
+// Tile width of a job's fused sweep; the energy partial sums follow it.
+static int set_tile(ea_ctx *c, int kt) {
+  JobDev &j = c->j;
+  if (kt == j.kt) return EA_OK;
+  const Geometry &g = c->g;
+  const size_t smem = (size_t)g.NB * 2560 + (size_t)3 * g.NB * kt * g.NR * 8 + (size_t)kt * 32;
+  if (smem > 227 * 1024) return fail(EA_ERR_ARG, "tile width %d needs %zu bytes of shared memory", kt, smem);
+  const int nt = (g.half + kt - 1) / kt;
+  if (nt > j.ntiles) {
+    int32_t *p = nullptr;
+    int rc = own(c, p, (size_t)nt * g.ns * g.NR * g.NB);
+    if (rc) return rc;
+    j.epart = p;
+  }
+  j.kt = kt;
+  j.ntiles = nt;
+  return EA_OK;
+}
+
+static int batch_kt(const ea_batch *b, int forced) {
+  const int c8[3] = {4, 2, 1}, c4[3] = {8, 4, 2}, c2[3] = {16, 8, 4};
+  const int *c = b->NR == 8 ? c8 : b->NR == 4 ? c4 : c2;
+  auto fits = [&](int kt) { return batch_sweep_smem(b->NR, kt, b->NBmax) <= 227 * 1024; };
+  if (forced) {
+    for (int i = 0; i < 3; ++i)
+      if (c[i] == forced && fits(forced)) return forced;
+    return 0;
+  }
+  for (int i = 0; i < 3; ++i) {
+    if (!fits(c[i])) continue;
+    long tiles = 0;
+    for (ea_ctx *x : b->jobs) tiles += (x->g.half + c[i] - 1) / c[i];
+    if (tiles >= 4 * 152) return c[i];
+  }
+  for (int i = 2; i >= 0; --i)
+    if (fits(c[i])) return c[i];
+  return 0;
+}
+
+// Uploads the jobs' descriptors and work lists when they changed.
+static int batch_upload(ea_batch *b) {
+  const int n = (int)b->jobs.size();
+  std::vector<JobDev> hj(n);
+  std::vector<uint32_t> hp((size_t)KB_COUNT * (n + 1), 0);
+  int slab_threads = 32;
+  for (int i = 0; i < n; ++i) {
+    hj[i] = b->jobs[i]->j;
+    hj[i].U = nullptr;
+    uint32_t cnt[KB_COUNT];
+    batch_blocks(hj[i], cnt);
+    for (int k = 0; k < KB_COUNT; ++k) hp[(size_t)k * (n + 1) + i + 1] = hp[(size_t)k * (n + 1) + i] + cnt[k];
+    int D, P, ns;
+    if (hj[i].nclust > 0 && slab_shape(hj[i], &D, &P, &ns)) {
+      const int t = hj[i].L * hj[i].L * P;
+      if (t > slab_threads) slab_threads = t;
+    }
+  }
+  const bool same = b->up_jobs.size() == hj.size() &&
+                    !std::memcmp(b->up_jobs.data(), hj.data(), sizeof(JobDev) * n) && b->up_pre == hp;
+  if (!same) {
+    // kernels of earlier bins may still read the arrays
+    CU(cudaStreamSynchronize(b->bs));
+    CU(cudaMemcpy(b->d_jobs, hj.data(), sizeof(JobDev) * n, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(b->d_pre, hp.data(), sizeof(uint32_t) * hp.size(), cudaMemcpyHostToDevice));
+    b->up_jobs = hj;
+    b->up_pre = hp;
+  }
+  b->bd.jobs = b->d_jobs;
+  b->bd.njobs = n;
+  for (int k = 0; k < KB_COUNT; ++k) {
+    b->bd.pre[k] = b->d_pre + (size_t)k * (n + 1);
+    b->bd.total[k] = hp[(size_t)k * (n + 1) + n];
+  }
+  b->bd.slab_threads = slab_threads;
+  return EA_OK;
+}
+
+int ea_batch_create(ea_ctx *const *jobs, int32_t njobs, int32_t tile, ea_batch **out) {
+  if (!jobs || !out || njobs < 1 || njobs > kBatchMaxJobs) return fail(EA_ERR_ARG, "1..%d jobs", kBatchMaxJobs);
+  ea_batch *b = new ea_batch();
+  for (int i = 0; i < njobs; ++i) {
+    ea_ctx *c = jobs[i];
+    if (!c) { delete b; return fail(EA_ERR_ARG, "null job %d", i); }
+    for (ea_ctx *o : b->jobs)
+      if (o == c) { delete b; return fail(EA_ERR_ARG, "job %d appears twice", i); }
+    if (i && (c->device != b->device || c->g.NR != b->NR)) {
+      delete b;
+      return fail(EA_ERR_ARG, "the jobs of a batch share the device and the number of replicas");
+    }
+    b->device = c->device;
+    b->NR = c->g.NR;
+    if (c->g.NB > b->NBmax) b->NBmax = c->g.NB;
+    b->jobs.push_back(c);
+  }
+  CU(cudaSetDevice(b->device));
+  b->KT = batch_kt(b, tile);
+  if (!b->KT) { delete b; return fail(EA_ERR_ARG, "no tile width fits NB=%d in shared memory", b->NBmax); }
+  for (ea_ctx *c : b->jobs) {
+    CU(cudaStreamSynchronize(c->st));
+    int rc = set_tile(c, b->KT);
+    if (rc) { delete b; return rc; }
+  }
+  cudaError_t e = batch_setup(b->NR, b->KT);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->bs, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_jobs, sizeof(JobDev) * njobs);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_pre, sizeof(uint32_t) * KB_COUNT * (njobs + 1));
+  if (e != cudaSuccess) { ea_batch_destroy(b); return fail(EA_ERR_CUDA, "batch set-up: %s", cudaGetErrorString(e)); }
+  *out = b;
+  return EA_OK;
+}
+
+int ea_batch_destroy(ea_batch *b) {
+  if (!b) return EA_OK;
+  cudaSetDevice(b->device);
+  if (b->bs) cudaStreamSynchronize(b->bs);
+  if (b->cycle) cudaGraphExecDestroy(b->cycle);
+  if (b->d_jobs) cudaFree(b->d_jobs);
+  if (b->d_pre) cudaFree(b->d_pre);
+  if (b->done) cudaEventDestroy(b->done);
+  if (b->bs) cudaStreamDestroy(b->bs);
+  delete b;
+  return EA_OK;
+}
+
+int ea_batch_tile(const ea_batch *b, int32_t *tile) {
+  if (!b || !tile) return fail(EA_ERR_ARG, "null argument");
+  *tile = b->KT;
+  return EA_OK;
+}
+
+// One tempering cycle for every job: ptfr sweeps (energy fused into the last
+// odd half-sweep), or an energy pass when ptfr is 0, then the swaps.
+static int batch_cycle_launch(ea_batch *b, int ptfr) {
+  for (int sw = 0; sw < ptfr; ++sw)
+    for (int p = 0; p < 2; ++p) {
+      CU(batch_fill_bits(b->bd, p, b->bs));
+      CU(batch_sweep(b->bd, b->NR, b->KT, b->NBmax, p, sw == ptfr - 1 && p == 1, true, b->bs));
+    }
+  if (ptfr == 0) CU(batch_sweep(b->bd, b->NR, b->KT, b->NBmax, 0, true, false, b->bs));
+  CU(batch_energy_reduce(b->bd, b->bs));
+  CU(batch_pt(b->bd, b->bs));
+  return EA_OK;
+}
+
+static int batch_cycle(ea_batch *b, int ptfr) {
+  if (!b->cycle || b->cycle_ptfr != ptfr) {
+    if (b->cycle) { cudaGraphExecDestroy(b->cycle); b->cycle = nullptr; }
+    cudaGraph_t graph = nullptr;
+    CU(cudaStreamBeginCapture(b->bs, cudaStreamCaptureModeThreadLocal));
+    const int rc = batch_cycle_launch(b, ptfr);
+    const cudaError_t e = cudaStreamEndCapture(b->bs, &graph);
+    if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
+    CU(e);
+    const cudaError_t ei = cudaGraphInstantiate(&b->cycle, graph, 0);
+    cudaGraphDestroy(graph);
+    CU(ei);
+    b->cycle_ptfr = ptfr;
+  }
+  CU(cudaGraphLaunch(b->cycle, b->bs));
+  return EA_OK;
+}
+
+static int batch_houdayer(ea_batch *b, int nclust) {
+  const int n = (int)b->jobs.size();
+  int rc;
+  for (ea_ctx *c : b->jobs)
+    if ((rc = houdayer_prepare(c, nclust))) return rc;
+  if ((rc = batch_upload(b))) return rc;
+  for (ea_ctx *c : b->jobs) CU(cudaStreamWaitEvent(b->bs, c->drawn[c->cur], 0));
+  CU(batch_pairs(b->bd, b->bs));
+  UTable &u = b->u;
+  for (int grp = 0; grp < 2; ++grp) {
+    for (int i = 0; i < n; ++i) u.u[i] = b->jobs[i]->U[b->jobs[i]->cur][grp];
+    CU(batch_houdayer_group(b->bd, u, grp, b->bs));
+    // jobs whose planes exceed the slab labelling take the one-job path
+    for (int i = 0; i < n; ++i) {
+      const uint32_t *pre = b->up_pre.data() + (size_t)KB_SLAB * (n + 1);
+      if (pre[i + 1] != pre[i]) continue;
+      JobDev jg = b->jobs[i]->j;
+      jg.U = u.u[i];
+      CU(launch_houdayer_group(jg, grp, b->bs));
+    }
+  }
+  for (ea_ctx *c : b->jobs)
+    if ((rc = houdayer_finish(c, b->bs))) return rc;
+  return EA_OK;
+}
+
+int ea_batch_run_bin(ea_batch *b, const ea_cadence *cad) {
+  if (!b || !cad || cad->itmax < 1 || cad->houfr < 1 || cad->mesfr < 1 || cad->ptfr < 0)
+    return fail(EA_ERR_ARG, "bad cadence");
+  CU(cudaSetDevice(b->device));
+  int frec, maxit;
+  trw(cad->itmax, &frec, &maxit);
+  // every job's earlier work comes first
+  for (ea_ctx *c : b->jobs) {
+    if (!c->have_temps) return fail(EA_ERR_STATE, "temperatures not set");
+    if (cad->cluster && c->g.NR < 4) return fail(EA_ERR_ARG, "the Houdayer move needs at least 2 replicas per group");
+    CU(cudaEventRecord(b->done, c->st));
+    CU(cudaStreamWaitEvent(b->bs, b->done, 0));
+  }
+  // buffers that grow are reallocated only once the batch's earlier kernels ended
+  bool grow = false;
+  for (ea_ctx *c : b->jobs)
+    grow = grow || maxit > c->hist_cap || (cad->cluster && norm_nclust(c->g, cad->nclust) > c->nclust_cap);
+  if (grow) CU(cudaStreamSynchronize(b->bs));
+  for (ea_ctx *c : b->jobs) {
+    const Geometry &g = c->g;
+    const size_t nsr = (size_t)g.ns * g.NR;
+    if (maxit > c->hist_cap) {
+      if (c->hist) cudaFree(c->hist);
+      c->hist = nullptr;
+      CU(dalloc(c->hist, nsr * maxit * g.NB));
+      c->hist_cap = maxit;
+    }
+    c->j.hist = c->hist;
+    c->j.maxit_trw = maxit;
+    CU(cudaMemsetAsync(c->avgE, 0, nsr * g.NB * 8, b->bs));
+    CU(cudaMemsetAsync(c->hist, 0, nsr * maxit * g.NB, b->bs));
+    if (cad->cluster) {
+      const int rc = ensure_cluster(c, norm_nclust(g, cad->nclust));
+      if (rc) return rc;
+    }
+  }
+  int rc = batch_upload(b);
+  if (rc) return rc;
+  for (int it = 0; it < cad->itmax; ++it) {
+    for (int im = 0; im < cad->mesfr; ++im) {
+      for (int ih = 0; ih < cad->houfr; ++ih) {
+        // with ptfr = 0 the cycle measures the energies before the swaps
+        // (measuring energies that are still fresh leaves them unchanged)
+        if ((rc = batch_cycle(b, cad->ptfr))) return rc;
+      }
+      if (cad->cluster && (rc = batch_houdayer(b, cad->nclust))) return rc;
+    }
+    CU(batch_sweep(b->bd, b->NR, b->KT, b->NBmax, 0, true, false, b->bs));
+    CU(batch_energy_reduce(b->bd, b->bs));
+    CU(batch_measure(b->bd, (it % frec == frec - 1) ? it / frec : -1, b->bs));
+  }
+  // later work of each job comes after the batch
+  CU(cudaEventRecord(b->done, b->bs));
+  for (ea_ctx *c : b->jobs) {
+    CU(cudaStreamWaitEvent(c->st, b->done, 0));
+    c->energies_fresh = true;
+  }
+  return EA_OK;
+}
+
+int ea_batch_sync(ea_batch *b) {
+  if (!b) return fail(EA_ERR_ARG, "null batch");
+  CU(cudaSetDevice(b->device));
+  CU(cudaStreamSynchronize(b->bs));
+  return EA_OK;
+}
+
+int ea_batch_stream(ea_batch *b, void **stream) {
+  if (!b || !stream) return fail(EA_ERR_ARG, "null argument");
+  *stream = (void *)b->bs;
+  return EA_OK;
+}
+
+int ea_bin_results(ea_ctx *c, double *avgE, uint8_t *hist, int32_t *maxit_trw) {
+  if (check(c)) return EA_ERR_ARG;
+  if (set_device(c)) return EA_ERR_CUDA;
+  const Geometry &g = c->g;
+  const size_t nsr = (size_t)g.ns * g.NR;
+  CU(cudaStreamSynchronize(c->st));
+  const int maxit = c->j.maxit_trw;
+  if (avgE) CU(cudaMemcpy(avgE, c->avgE, nsr * g.NB * 8, cudaMemcpyDeviceToHost));
+  if (hist && c->hist) CU(cudaMemcpy(hist, c->hist, nsr * maxit * g.NB, cudaMemcpyDeviceToHost));
+  if (maxit_trw) *maxit_trw = maxit;
+  return ea_check_exact(c);
 }
 
 }  // extern "C"

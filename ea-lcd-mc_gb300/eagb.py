@@ -223,6 +223,16 @@ class Job:
         cad = Cadence(itmax, houfr, mesfr, ptfr, int(cluster), nclust)
         _ck(lib().ea_run_bin(self.ctx, C.byref(cad), None, None, None))
 
+    def bin_results(self):
+        """Energy averages and temperature history of the last bin (plain or batched)."""
+        avg = np.zeros((self.g.nsamples, self.g.nrep, self.g.nbetas))
+        hist = np.zeros(self.g.nsamples * self.g.nrep * 512 * self.g.nbetas, np.uint8)
+        mx = C.c_int32(0)
+        _ck(lib().ea_bin_results(self.ctx, P(avg), P(hist), C.byref(mx)))
+        m = mx.value
+        return avg, hist[:self.g.nsamples * self.g.nrep * m * self.g.nbetas].reshape(
+            self.g.nsamples, self.g.nrep, m, self.g.nbetas)
+
     def check_exact(self):
         _ck(lib().ea_check_exact(self.ctx))
 
@@ -252,6 +262,40 @@ def curand_uniforms(seed, offset, n, device=0):
     out = np.zeros(n, np.float64)
     _ck(lib().ea_curand_uniforms(device, C.c_uint64(seed), C.c_uint64(offset), C.c_uint64(n), P(out)))
     return out
+
+
+class Batch:
+    """Many jobs advanced together by the persistent batched kernels."""
+
+    def __init__(self, jobs, tile=0):
+        self.jobs = list(jobs)
+        arr = (C.c_void_p * len(self.jobs))(*[j.ctx.value if isinstance(j.ctx, C.c_void_p) else j.ctx
+                                              for j in self.jobs])
+        self.b = C.c_void_p()
+        _ck(lib().ea_batch_create(arr, len(self.jobs), int(tile), C.byref(self.b)))
+
+    def tile(self):
+        v = C.c_int32()
+        _ck(lib().ea_batch_tile(self.b, C.byref(v)))
+        return v.value
+
+    def run_bin(self, itmax, houfr, mesfr, ptfr, cluster=True, nclust=0):
+        """Enqueue one bin for every job (asynchronous)."""
+        cad = Cadence(itmax, houfr, mesfr, ptfr, int(cluster), nclust)
+        _ck(lib().ea_batch_run_bin(self.b, C.byref(cad)))
+
+    def sync(self):
+        _ck(lib().ea_batch_sync(self.b))
+
+    def stream(self):
+        v = C.c_void_p()
+        _ck(lib().ea_batch_stream(self.b, C.byref(v)))
+        return v.value
+
+    def close(self):
+        if self.b:
+            _ck(lib().ea_batch_destroy(self.b))
+            self.b = None
 
 
 def new_job(L, Lz, betas, cum, nsamples=1, NR=8, bc=EA_OBC, masters=(1, 2, 3, 4), list_samples=None,

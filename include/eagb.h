@@ -206,6 +206,30 @@ int ea_get_rng_sms(const ea_ctx *ctx, int32_t *nsm);
  * avgE [nsamples][NR][NB] (sum over it, beta order) and hist [nsamples][NR][maxit][NB]
  * may be NULL; maxit_trw = itmax / frecTRW (io.c:431-434). */
 int ea_run_bin(ea_ctx *ctx, const ea_cadence *cad, double *avgE, uint8_t *hist, int32_t *maxit_trw);
+/* Energy averages, temperature history and maxit_trw of the job's last bin
+ * (by ea_run_bin or a batch), as ea_run_bin returns them. */
+int ea_bin_results(ea_ctx *ctx, double *avgE, uint8_t *hist, int32_t *maxit_trw);
+
+/* Batches.  A batch advances many jobs -- of different L, Lz, boundary
+ * condition, number of temperatures and samples, same number of replicas and
+ * device -- with one persistent kernel launch per step for all of them (a
+ * packed work list of (job, block) items); the sweep / energy / tempering
+ * cycle is replayed as a CUDA graph.  Each job's words, energies, swaps and
+ * uniforms are those of ea_run_bin on the job alone.  The batch fixes the
+ * jobs' sweep tile width (tile = 0: chosen from the work list; else 1, 2, 4,
+ * 8 or 16 as the replica count allows).  A job's own calls may be used
+ * between batch calls; they are ordered after the batch.  No reference
+ * counterpart: the reference runs one job per process. */
+typedef struct ea_batch ea_batch;
+int ea_batch_create(ea_ctx *const *jobs, int32_t njobs, int32_t tile, ea_batch **out);
+int ea_batch_destroy(ea_batch *b);
+int ea_batch_tile(const ea_batch *b, int32_t *tile);
+/* One bin of the cadence for every job, enqueued without a host
+ * synchronisation; read each job's results with ea_bin_results. */
+int ea_batch_run_bin(ea_batch *b, const ea_cadence *cad);
+int ea_batch_sync(ea_batch *b);
+/* The batch's CUDA stream (a cudaStream_t). */
+int ea_batch_stream(ea_batch *b, void **stream);
 /* With avgE and hist both NULL, ea_run_bin only enqueues the bin and returns
  * without synchronising; ea_check_exact then synchronises and reports
  * EA_ERR_INEXACT if any tempering decision fell outside the exact exp table. */
