@@ -31,6 +31,11 @@ L, LZ, NR, NS, HOUFR = 24, 192, 8, 31, 5
 LUT = os.path.join(ROOT, "tests", "golden", "lut_T06_16_N32.npz")
 MASTERS = (0x1234567890ABCDEF, 0x0FEDCBA987654321, 0x1111222233334444, 0x5555666677778888)
 WORKLOAD = "L24_Lz192_OBC_NB32_NR8_ns31_ptfr1_houfr5"
+# mixed-geometry workload of the batched vs plain comparison: every
+# L x (Lz/L) x boundary x NT combination is one job class
+# (36 geometry classes; either 36 jobs of 32 samples or 288 jobs of 4)
+MIX_L, MIX_RATIO, MIX_NT, MIX_NR, MIX_HOUFR = (8, 16), (2, 4, 8), (16, 24, 32), 4, 10
+MIX_WORKLOAD = "mixed_L8-16_Lz2-8L_PBC-OBC_NT16-32_NR4_ns%d_ptfr1_houfr10"
 
 
 def load_eagb():
@@ -136,6 +141,86 @@ def run_reference(args, rank, world):
                              "sample": "1 sample x 1 Metropolis sweep of L24 Lz192 NB32 NR8 per step, oracle C restatement, OpenMP"},
             "e2e": {"value": value, "unit": "spin-updates/ps", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def mixed_jobs(eagb, dev, ns, copies):
+    jobs = []
+    for _ in range(copies):
+        for L in MIX_L:
+            for ratio in MIX_RATIO:
+                for bc in (eagb.EA_PBC, eagb.EA_OBC):
+                    for nt in MIX_NT:
+                        d = np.load(os.path.join(ROOT, "tests", "golden", "lut_T07_16_N%d.npz" % nt))
+                        k = len(jobs)
+                        m = tuple((x ^ (0x9E3779B97F4A7C15 * (k + 1))) & 0xFFFFFFFFFFFFFFFF or 1 for x in MASTERS)
+                        job = eagb.new_job(L, ratio * L, d["betas"], d["cum"], nsamples=ns, NR=MIX_NR, bc=bc,
+                                           masters=m, device=dev, jobid=k)
+                        job.set_rng_sms(0)
+                        jobs.append(job)
+    return jobs
+
+
+def run_mixed(args, dev, torch, eagb, ns, copies):
+    """Batched persistent form vs plain form (one job per launch sequence, every
+    job on its own stream, all enqueued before waiting) on the same mixed
+    workload, from twin initial states; one step = one bin of itmax=1 for
+    every job.  Inputs (spins + uniforms) are far larger than L2."""
+    su_step = 0
+    plain, batched = mixed_jobs(eagb, dev, ns, copies), mixed_jobs(eagb, dev, ns, copies)
+    for j in plain:
+        su_step += MIX_HOUFR * j.g.L * j.g.L * j.g.Lz * MIX_NR * j.g.nbetas * ns
+    batch = eagb.Batch(batched)
+    s0 = torch.cuda.Stream(device=dev)
+    cad = dict(itmax=1, houfr=MIX_HOUFR, mesfr=1, ptfr=1)
+
+    def timed(jobs, enqueue, steps):
+        streams = [torch.cuda.ExternalStream(j.stream(), device=dev) for j in jobs]
+        torch.cuda.synchronize(dev)
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(s0)
+        for st in streams:
+            st.wait_event(t0)
+        for _ in range(steps):
+            enqueue()
+        for j, st in zip(jobs, streams):
+            j.join()
+            e = torch.cuda.Event()
+            e.record(st)
+            s0.wait_event(e)
+        t1.record(s0)
+        torch.cuda.synchronize(dev)
+        return t0.elapsed_time(t1)
+
+    def plain_step():
+        for j in plain:
+            j.run_cycles(**cad)
+
+    def batch_step():
+        batch.run_bin(**cad)
+
+    timed(plain, plain_step, args.warmup)
+    timed(batched, batch_step, args.warmup)
+    ms_plain = timed(plain, plain_step, args.steps)
+    ms_batch = timed(batched, batch_step, args.steps)
+    same = True
+    for a, b in zip(plain, batched):
+        for smp in range(ns):
+            ea, oa = a.get_spins(smp)
+            eb, ob = b.get_spins(smp)
+            same = same and np.array_equal(ea, eb) and np.array_equal(oa, ob)
+        same = same and np.array_equal(a.bin_results()[0], b.bin_results()[0])
+    tile = batch.tile()
+    batch.close()
+    for j in plain + batched:
+        j.close()
+    vp = su_step * args.steps / (ms_plain * 1e-3) / 1e12
+    vb = su_step * args.steps / (ms_batch * 1e-3) / 1e12
+    return {"workload": MIX_WORKLOAD % ns, "jobs": len(plain), "unit": "spin-updates/ps",
+            "plain_value": vp, "batched_value": vb, "speedup": vb / vp,
+            "plain_ms_per_step": ms_plain / args.steps, "batched_ms_per_step": ms_batch / args.steps,
+            "spin_updates_per_step": su_step, "bit_exact_plain_vs_batched": bool(same), "tile": tile,
+            "graph": "sweep/energy/tempering cycle replayed as a CUDA graph",
+            "l2": "inputs larger than L2 (spins ~0.3 GB, uniforms ~9 GB)"}
 
 
 def run_ours(args, rank, world, local):
@@ -260,6 +345,8 @@ def run_ours(args, rank, world, local):
                       "uniforms_overlapped": rg_ms.value, "step_total": ms},
         "clocks": clk.summary(),
     }
+    if not args.no_mixed:
+        line["batched"] = [run_mixed(args, dev, torch, eagb, 4, 8), run_mixed(args, dev, torch, eagb, 32, 1)]
     if not args.no_cpu:
         su, dt = cpu_sample(os.cpu_count() or 1, sweeps=20)
         line["cpu_baseline"] = {"value": su / dt / 1e12, "unit": "spin-updates/ps", "cores": os.cpu_count(),
@@ -269,12 +356,16 @@ def run_ours(args, rank, world, local):
 
 
 def main():
+    # more hardware queues, so that the plain form's per-job streams and the
+    # per-job cluster-uniform generators can run side by side
+    os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the batched vs plain mixed-geometry leg")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

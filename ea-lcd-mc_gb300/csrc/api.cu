@@ -7,6 +7,7 @@
 #include <cuda.h>
 #include <curand.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -80,6 +81,7 @@ struct ea_ctx {
   int cur = 0;    // set that holds the uniforms of the next move
   int ready = 0;  // sets drawn and not yet used by a move (0..2)
   uint32_t *label = nullptr;
+  uint32_t *sel = nullptr;
   unsigned long long *Q = nullptr;
   // measurement buffers
   double *avgE = nullptr;
@@ -446,6 +448,7 @@ int ea_destroy(ea_ctx *c) {
   c->st = nullptr;
   drop_partition(c);
   if (c->label) cudaFree(c->label);
+  if (c->sel) cudaFree(c->sel);
   if (c->Q) cudaFree(c->Q);
   if (c->hist) cudaFree(c->hist);
   if (c->exptab) cudaFree(c->exptab);
@@ -755,13 +758,16 @@ static int ensure_cluster(ea_ctx *c, int nclust) {
   if (nclust > c->nclust_cap) {
     CU(cudaStreamSynchronize(c->st));
     if (c->label) cudaFree(c->label);
+    if (c->sel) cudaFree(c->sel);
     if (c->Q) cudaFree(c->Q);
-    c->label = nullptr; c->Q = nullptr;
+    c->label = nullptr; c->sel = nullptr; c->Q = nullptr;
     CU(dalloc(c->label, (size_t)g.V * nclust * g.ns));
+    CU(dalloc(c->sel, (size_t)g.V / 32 * nclust * g.ns));
     CU(dalloc(c->Q, (size_t)2 * g.half * nclust * g.ns));
     c->nclust_cap = nclust;
   }
   c->j.label = c->label;
+  c->j.sel = c->sel;
   c->j.Q = c->Q;
   c->j.nclust = nclust;
   set_dividers(c->j);
@@ -962,12 +968,14 @@ struct ea_batch {
   cudaEvent_t done = nullptr;
   JobDev *d_jobs = nullptr;
   uint32_t *d_pre = nullptr;
+  uint32_t *d_ctr = nullptr;
   std::vector<JobDev> up_jobs;  // JobDev array as last uploaded
   std::vector<uint32_t> up_pre;
   BatchDev bd{};
   cudaGraphExec_t cycle = nullptr;
   int cycle_ptfr = -1;
   UTable u{};  // uniforms of the current group, by job
+  float tuned_ms = 0.f;  // autotuner: two sweeps of the chosen tile width
 };
 
 extern "C" {
@@ -994,7 +1002,7 @@ static int set_tile(ea_ctx *c, int kt) {
 static int batch_kt(const ea_batch *b, int forced) {
   const int c8[3] = {4, 2, 1}, c4[3] = {8, 4, 2}, c2[3] = {16, 8, 4};
   const int *c = b->NR == 8 ? c8 : b->NR == 4 ? c4 : c2;
-  auto fits = [&](int kt) { return batch_sweep_smem(b->NR, kt, b->NBmax) <= 227 * 1024; };
+  auto fits = [&](int kt) { return batch_sweep_smem(b->NR, kt, b->NBmax) <= 227 * 1024 - 256; };
   if (forced) {
     for (int i = 0; i < 3; ++i)
       if (c[i] == forced && fits(forced)) return forced;
@@ -1016,17 +1024,19 @@ static int batch_upload(ea_batch *b) {
   const int n = (int)b->jobs.size();
   std::vector<JobDev> hj(n);
   std::vector<uint32_t> hp((size_t)KB_COUNT * (n + 1), 0);
-  int slab_threads = 32;
+  int slab_threads = 32, flip_smem = 0;
   for (int i = 0; i < n; ++i) {
     hj[i] = b->jobs[i]->j;
     hj[i].U = nullptr;
     uint32_t cnt[KB_COUNT];
     batch_blocks(hj[i], cnt);
     for (int k = 0; k < KB_COUNT; ++k) hp[(size_t)k * (n + 1) + i + 1] = hp[(size_t)k * (n + 1) + i] + cnt[k];
-    int D, P, ns;
-    if (hj[i].nclust > 0 && slab_shape(hj[i], &D, &P, &ns)) {
+    if (cnt[KB_SLAB]) {
+      int D, P, ns;
+      slab_shape(hj[i], &D, &P, &ns);
       const int t = hj[i].L * hj[i].L * P;
       if (t > slab_threads) slab_threads = t;
+      if ((int)flip_smem_bytes(hj[i]) > flip_smem) flip_smem = (int)flip_smem_bytes(hj[i]);
     }
   }
   const bool same = b->up_jobs.size() == hj.size() &&
@@ -1046,7 +1056,91 @@ static int batch_upload(ea_batch *b) {
     b->bd.total[k] = hp[(size_t)k * (n + 1) + n];
   }
   b->bd.slab_threads = slab_threads;
+  b->bd.flip_smem = flip_smem;
+  b->bd.ctr = b->d_ctr;
+  // chunks of work items a block takes at a time: one heavy item, or several
+  // light ones so that the job lookup and the fetch are amortised
+  const uint32_t chunk[KB_COUNT] = {1, 4, 1, 4, 4, 1, 4, 4, 1};
+  for (int k = 0; k < KB_COUNT; ++k) b->bd.chunk[k] = chunk[k];
+  if (b->bd.total[KB_SWEEP] >= 8u * 304u) b->bd.chunk[KB_SWEEP] = 2;
   return EA_OK;
+}
+
+// Autotuner: times the batched half-sweeps of every tile width that fits, on
+// the batch's own jobs, and keeps the fastest.  What the timing sweeps change
+// (spin words, half-sweep counter, Philox counters, the two generators that
+// feed them) is copied aside on the device first and put back after, so the
+// jobs are left exactly as they were.
+static int batch_autotune(ea_batch *b, float *best_ms) {
+  const int c8[3] = {4, 2, 1}, c4[3] = {8, 4, 2}, c2[3] = {16, 8, 4};
+  const int *c = b->NR == 8 ? c8 : b->NR == 4 ? c4 : c2;
+  std::vector<int> cand;
+  for (int i = 0; i < 3; ++i)
+    if (batch_sweep_smem(b->NR, c[i], b->NBmax) <= 227 * 1024 - 256) cand.push_back(c[i]);
+  if (cand.empty()) return fail(EA_ERR_ARG, "no tile width fits NB=%d in shared memory", b->NBmax);
+  b->KT = cand[0];
+  if (cand.size() == 1) return EA_OK;
+  struct Part { void *p; size_t n; };
+  std::vector<Part> parts;
+  size_t total = 0;
+  for (ea_ctx *x : b->jobs) {
+    const Geometry &g = x->g;
+    parts.push_back({x->j.spins, (size_t)g.ns * g.words_per_sample() * 8});
+    parts.push_back({x->j.iter, 8});
+    parts.push_back({x->j.ctr, sizeof(uint4) * g.NR});
+    parts.push_back({x->j.prc, sizeof(ea_hq) * g.NR});
+    parts.push_back({x->j.xo, sizeof(ea_xoshiro) * g.NR});
+  }
+  for (const Part &q : parts) total += (q.n + 255) & ~(size_t)255;
+  char *save = nullptr;
+  CU(cudaMalloc((void **)&save, total));
+  size_t off = 0;
+  for (const Part &q : parts) {
+    CU(cudaMemcpyAsync(save + off, q.p, q.n, cudaMemcpyDeviceToDevice, b->bs));
+    off += (q.n + 255) & ~(size_t)255;
+  }
+  cudaEvent_t e0, e1;
+  CU(cudaEventCreate(&e0));
+  CU(cudaEventCreate(&e1));
+  int best = cand[0];
+  float bms = 1e30f;
+  int rc = EA_OK;
+  for (int kt : cand) {
+    for (ea_ctx *x : b->jobs)
+      if ((rc = set_tile(x, kt))) break;
+    if (rc || (rc = batch_upload(b))) break;
+    if (batch_setup(b->NR, kt) != cudaSuccess) continue;
+    float ms = 0.f;
+    for (int rep = 0; rep < 2; ++rep) {  // the first pass warms up
+      cudaEventRecord(e0, b->bs);
+      for (int cyc = 0; cyc < 2; ++cyc)
+        for (int p = 0; p < 2; ++p) {
+          batch_fill_bits(b->bd, p, b->bs);
+          batch_sweep(b->bd, b->NR, kt, b->NBmax, p, p == 1, true, b->bs);
+        }
+      cudaEventRecord(e1, b->bs);
+      cudaEventSynchronize(e1);
+      cudaEventElapsedTime(&ms, e0, e1);
+    }
+    if (cudaGetLastError() != cudaSuccess) continue;
+    if (ms < bms) { bms = ms; best = kt; }
+  }
+  off = 0;
+  for (const Part &q : parts) {
+    cudaMemcpyAsync(q.p, save + off, q.n, cudaMemcpyDeviceToDevice, b->bs);
+    off += (q.n + 255) & ~(size_t)255;
+  }
+  cudaStreamSynchronize(b->bs);
+  cudaFree(save);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  b->KT = best;
+  for (ea_ctx *x : b->jobs)
+    if ((rc = set_tile(x, best))) return rc;
+  if (best_ms) *best_ms = bms;
+  CU(batch_setup(b->NR, best));
+  return batch_upload(b);
 }
 
 int ea_batch_create(ea_ctx *const *jobs, int32_t njobs, int32_t tile, ea_batch **out) {
@@ -1067,19 +1161,33 @@ int ea_batch_create(ea_ctx *const *jobs, int32_t njobs, int32_t tile, ea_batch *
     b->jobs.push_back(c);
   }
   CU(cudaSetDevice(b->device));
-  b->KT = batch_kt(b, tile);
-  if (!b->KT) { delete b; return fail(EA_ERR_ARG, "no tile width fits NB=%d in shared memory", b->NBmax); }
+  // heaviest work items first (a sweep tile costs ~ NB x samples), so that
+  // blocks drawing items in order end together
+  std::stable_sort(b->jobs.begin(), b->jobs.end(),
+                   [](const ea_ctx *x, const ea_ctx *y) { return x->g.NB * x->g.ns > y->g.NB * y->g.ns; });
+  if (tile) {
+    b->KT = batch_kt(b, tile);
+    if (!b->KT) { delete b; return fail(EA_ERR_ARG, "tile width %d does not fit NR=%d, NB=%d", tile, b->NR, b->NBmax); }
+  }
   for (ea_ctx *c : b->jobs) {
     CU(cudaStreamSynchronize(c->st));
-    int rc = set_tile(c, b->KT);
-    if (rc) { delete b; return rc; }
+    if (tile) {
+      int rc = set_tile(c, b->KT);
+      if (rc) { delete b; return rc; }
+    }
   }
-  cudaError_t e = batch_setup(b->NR, b->KT);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->bs, cudaStreamNonBlocking);
+  cudaError_t e = cudaStreamCreateWithFlags(&b->bs, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_jobs, sizeof(JobDev) * njobs);
   if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_pre, sizeof(uint32_t) * KB_COUNT * (njobs + 1));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_ctr, sizeof(uint32_t) * KB_COUNT);
+  if (e == cudaSuccess) e = cudaMemset(b->d_ctr, 0, sizeof(uint32_t) * KB_COUNT);
+  if (e == cudaSuccess && tile) e = batch_setup(b->NR, b->KT);
   if (e != cudaSuccess) { ea_batch_destroy(b); return fail(EA_ERR_CUDA, "batch set-up: %s", cudaGetErrorString(e)); }
+  if (!tile) {
+    int rc = batch_autotune(b, &b->tuned_ms);
+    if (rc) { ea_batch_destroy(b); return rc; }
+  }
   *out = b;
   return EA_OK;
 }
@@ -1091,6 +1199,7 @@ int ea_batch_destroy(ea_batch *b) {
   if (b->cycle) cudaGraphExecDestroy(b->cycle);
   if (b->d_jobs) cudaFree(b->d_jobs);
   if (b->d_pre) cudaFree(b->d_pre);
+  if (b->d_ctr) cudaFree(b->d_ctr);
   if (b->done) cudaEventDestroy(b->done);
   if (b->bs) cudaStreamDestroy(b->bs);
   delete b;

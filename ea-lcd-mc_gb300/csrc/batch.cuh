@@ -9,18 +9,24 @@
 namespace eagb {
 
 // Work-list kinds: the blocks of one job for each one-job kernel.
-enum { KB_SWEEP = 0, KB_REDUCE, KB_PT, KB_MEASURE, KB_OVERLAP, KB_SLAB, KB_MERGE, KB_APPLY, KB_COUNT };
+enum { KB_SWEEP = 0, KB_REDUCE, KB_PT, KB_MEASURE, KB_OVERLAP, KB_SLAB, KB_MERGE, KB_COMPRESS, KB_FLIP, KB_COUNT };
 
 constexpr int kBatchMaxJobs = 1024;
 
 // Device view of a batch (kernel parameter).  pre[k] is the exclusive prefix
 // sum over jobs of their block counts for kind k ([njobs + 1] entries).
+// Blocks take work from ctr[k] in chunks of chunk[k] items; the counter
+// returns to 0 by itself at the end of every launch (see item fetching in
+// batch.cu), so launches replay from a CUDA graph without resets.
 struct BatchDev {
   const JobDev *jobs;
   int njobs;
   const uint32_t *pre[KB_COUNT];
   uint32_t total[KB_COUNT];
+  uint32_t chunk[KB_COUNT];
+  uint32_t *ctr;     // [KB_COUNT] work counters
   int slab_threads;  // block size of the slab labelling (largest L^2 * P)
+  int flip_smem;     // dynamic SMEM of the flip (largest lattice)
 };
 
 // Uniforms of the current group for every job (kernel parameter).
@@ -30,9 +36,6 @@ struct UTable {
 
 // Blocks of job j for each kind (the one-job launch geometry, flattened).
 void batch_blocks(const JobDev &j, uint32_t out[KB_COUNT]);
-// Slab labelling shape of a job: planes per slab D, planes per pass P and
-// the number of slabs; false when the job needs the generic labelling.
-bool slab_shape(const JobDev &j, int *D, int *P, int *nslab);
 
 int batch_sweep_smem(int NR, int KT, int NBmax);
 // Kernel attributes and device figures the launchers use; called before any

@@ -6,6 +6,18 @@
 
 namespace eagb {
 
+bool slab_shape(const JobDev &j, int *D, int *P, int *nslab) {
+  const int S = j.L * j.L;
+  if (S > 1024) return false;
+  const int d = j.Lz < kSlabSites / S ? j.Lz : kSlabSites / S;
+  int p = 512 / S;
+  if (p > d) p = d;
+  if (p < 1) p = 1;
+  if ((d + p - 1) / p > kSlabMaxPerThread) return false;
+  *D = d; *P = p; *nslab = (j.Lz + d - 1) / d;
+  return true;
+}
+
 void set_dividers(JobDev &j) {
   j.fd_L.set(j.L); j.fd_S.set(j.L * j.L); j.fd_ml.set(j.msc_l); j.fd_mlz.set(j.msc_lz);
   j.fd_hl.set(j.msc_l / 2); j.fd_nclust.set(j.nclust > 0 ? j.nclust : 1);
@@ -39,7 +51,7 @@ __global__ void k_hou_overlap(const __grid_constant__ JobDev j, int g) {
   overlap_body(j, g, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
 }
 
-__global__ void __launch_bounds__(1024) k_cc_slab(const __grid_constant__ JobDev j, int D, int P) {
+__global__ void __launch_bounds__(1024, 2) k_cc_slab(const __grid_constant__ JobDev j, int D, int P) {
   __shared__ uint32_t lab[kSlabSites];
   __shared__ uint8_t qs[kSlabSites];
   cc_slab_body(j, D, P, blockIdx.x, blockIdx.y, lab, qs);
@@ -49,9 +61,24 @@ __global__ void k_cc_merge(const __grid_constant__ JobDev j, int D, int nslab) {
   cc_merge_body(j, D, nslab, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
 }
 
+__global__ void k_cc_compress(const __grid_constant__ JobDev j, int D, int nslab) {
+  cc_compress_body(j, D, nslab, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
+}
+
+__global__ void __launch_bounds__(512) k_hou_flip(const __grid_constant__ JobDev j, int g) {
+  extern __shared__ uint32_t s_flip[];
+  flip_body(j, j.U, g, blockIdx.x, s_flip + 64, reinterpret_cast<int *>(s_flip));
+}
+
+size_t flip_smem_bytes(const JobDev &j) { return 256 + (size_t)j.V / 8; }
+
+__global__ void __launch_bounds__(256) k_hou_select(const __grid_constant__ JobDev j) {
+  select_body(j, j.U, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y);
+}
+
 __global__ void __launch_bounds__(256) k_hou_apply(const __grid_constant__ JobDev j, int g) {
   __shared__ unsigned s_sel[8];
-  apply_body(j, j.U, g, blockIdx.x, blockIdx.y, s_sel);
+  apply_body(j, g, blockIdx.x, blockIdx.y, s_sel);
 }
 
 // Bonds between equal-overlap neighbours towards -x, -y (periodic) and -z
@@ -219,22 +246,36 @@ cudaError_t launch_houdayer_group(const JobDev &j, int g, cudaStream_t st) {
   const unsigned bw = (unsigned)((nw + 255) / 256), bs = (unsigned)((ns + 255) / 256);
   const unsigned nlat = (unsigned)(j.ns * j.nclust);
   k_hou_overlap<<<dim3((2 * j.half + 255) / 256, nlat), 256, 0, st>>>(j, g);
-  const int S = j.L * j.L;
-  if (S <= kSlabSites) {
-    const int D = min(j.Lz, kSlabSites / S), nslab = (j.Lz + D - 1) / D;
-    const int P = max(1, min(D, 512 / S));
-    if (S <= 1024 && (D + P - 1) / P <= kSlabMaxPerThread) {
-      k_cc_slab<<<dim3(nslab, j.ns * j.nclust), S * P, 0, st>>>(j, D, P);
-    } else {
-      k_cc_local<<<dim3(nslab, j.ns * j.nclust), 512, 0, st>>>(j, D);
+  int D, P, nslab;
+  if (slab_shape(j, &D, &P, &nslab)) {
+    k_cc_slab<<<dim3(nslab, nlat), j.L * j.L * P, 0, st>>>(j, D, P);
+    k_cc_merge<<<dim3((nslab * j.L * j.L + 255) / 256, nlat), 256, 0, st>>>(j, D, nslab);
+    k_cc_compress<<<dim3((nslab * j.L * j.L + 255) / 256, nlat), 256, 0, st>>>(j, D, nslab);
+    const size_t sm = flip_smem_bytes(j);
+    if (sm <= kFlipMaxSmem) {
+      static bool attr = false;
+      if (!attr) {
+        cudaFuncSetAttribute(k_hou_flip, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFlipMaxSmem);
+        attr = true;
+      }
+      k_hou_flip<<<nlat, 512, sm, st>>>(j, g);
+      return cudaGetLastError();
     }
-    k_cc_merge<<<dim3((nslab * S + 255) / 256, nlat), 256, 0, st>>>(j, D, nslab);
   } else {
-    // planes too large for SMEM: Komura's passes on global labels
-    k_cc_init<<<bs, 256, 0, st>>>(j);
-    k_cc_flatten<<<bs, 256, 0, st>>>(j);
-    k_cc_union<<<bs, 256, 0, st>>>(j);
+    const int S = j.L * j.L;
+    if (S <= kSlabSites) {
+      D = min(j.Lz, kSlabSites / S);
+      nslab = (j.Lz + D - 1) / D;
+      k_cc_local<<<dim3(nslab, nlat), 512, 0, st>>>(j, D);
+      k_cc_merge<<<dim3((nslab * S + 255) / 256, nlat), 256, 0, st>>>(j, D, nslab);
+    } else {
+      // planes too large for SMEM: Komura's passes on global labels
+      k_cc_init<<<bs, 256, 0, st>>>(j);
+      k_cc_flatten<<<bs, 256, 0, st>>>(j);
+      k_cc_union<<<bs, 256, 0, st>>>(j);
+    }
   }
+  k_hou_select<<<dim3((j.V + 255) / 256, nlat), 256, 0, st>>>(j);
   k_hou_apply<<<dim3((2 * j.half + 3) / 4, nlat), 256, 0, st>>>(j, g);
   return cudaGetLastError();
 }

@@ -63,7 +63,8 @@ struct JobDev {
   ea_hq *rc;
   int32_t *pairs;                   // [2 groups][2]
   unsigned long long *Q;            // [s][nclust][2][half] overlap words
-  uint32_t *label;                  // [s][nclust][V]
+  uint32_t *label;                  // [s][nclust][V] natural order
+  uint32_t *sel;                    // [s][nclust][V / 32] cluster selection bits, natural order
   const double *U;                  // [s][NB][V] uniforms of the current group
   int nclust;
   // x coordinate against which site 0 tests its periodic -x bond.  The
@@ -74,6 +75,19 @@ struct JobDev {
   // dividers of the site <-> multispin-word maps
   FastDiv fd_L, fd_S, fd_ml, fd_mlz, fd_hl, fd_nclust;
 };
+
+constexpr int kSlabSites = 8192;        // sites of a slab held in SMEM
+constexpr int kSlabMaxPerThread = 16;   // sites a thread of the slab labelling owns
+
+// Shared memory of the one-CTA-per-lattice selection and flip (V/8 bytes of
+// selection bits + the 64 bit offsets); larger lattices take the two-kernel
+// path (global selection bits).
+constexpr size_t kFlipMaxSmem = 200 * 1024;
+size_t flip_smem_bytes(const JobDev &j);
+
+// Slab labelling shape of a job: planes per slab D, planes per pass P and the
+// number of slabs; false when its planes need the generic labelling.
+bool slab_shape(const JobDev &j, int *D, int *P, int *nslab);
 
 // Fills the dividers of j from its sizes (nclust included).
 void set_dividers(JobDev &j);

@@ -159,7 +159,10 @@ __device__ __forceinline__ u64 flip_mask(const u64 f[6], u64 b0, u64 b1, u64 b2)
 // energy of the updated words (each bond has exactly one end on each parity).
 // ---------------------------------------------------------------------------
 template <int NR, int KT, bool UPDATE>
-__device__ __forceinline__ void sweep_body(const JobDev &j, int tile, int parity, int energy, unsigned char *smem) {
+// stage = false: the thresholds of this job are already in SMEM (the block's
+// previous tile was of the same job).
+__device__ __forceinline__ void sweep_body(const JobDev &j, int tile, int parity, int energy, unsigned char *smem,
+                                           bool stage = true) {
   const int NB = j.NB, half = j.half;
   u64 *s_cum = reinterpret_cast<u64 *>(smem);
   uint16_t *s_pre = reinterpret_cast<uint16_t *>(s_cum + (UPDATE ? NB * 256 : 0));
@@ -168,7 +171,7 @@ __device__ __forceinline__ void sweep_body(const JobDev &j, int tile, int parity
   const int k0 = tile * KT;
   const int tid = threadIdx.x, nth = blockDim.x;
 
-  if (UPDATE) {
+  if (UPDATE && stage) {
     const uint4 *cs = reinterpret_cast<const uint4 *>(j.cum);
     uint4 *cd = reinterpret_cast<uint4 *>(s_cum);
     for (int i = tid; i < NB * 128; i += nth) cd[i] = cs[i];
@@ -414,7 +417,6 @@ __device__ __forceinline__ void cc_unite(uint32_t *lab, uint32_t a, uint32_t b) 
 // planes of one (sample, beta) lattice in SMEM.  Local index order is natural
 // order shifted by z0 L^2, so a slab root is the smallest global index of its
 // slab piece; only bonds between slabs are left for k_cc_merge.
-constexpr int kSlabSites = 8192;
 
 // Planes of up to 1024 sites: one thread per (x, y) column and P planes
 // (at most 16 sites a thread), in lock-step rounds so that no lane walks a
@@ -427,7 +429,6 @@ constexpr int kSlabSites = 8192;
 // smallest index of its slab cluster.  The bonds are those of the union-find
 // of the reference (HoudayerXEA.cu:77-121): -x and -y periodic, -z inside the
 // slab.
-constexpr int kSlabMaxPerThread = 16;
 
 // Threads from S*P on (a batched launch sized for a larger plane) own no
 // sites and only take part in the barriers.
@@ -523,10 +524,102 @@ __device__ __forceinline__ void cc_merge_body(const JobDev &j, int D, int nslab,
     cc_unite(j.label + lat * j.V, (uint32_t)(xy + S * z), (uint32_t)(xy + S * zm));
 }
 
-// q' = q xor [U(root) < 0.5] packed back into words, then s_r1 ^= q', s_r2 ^= q'
-// (HoudayerXEA.cu:54-75,358-374; main.cu:776-832,938-991).  Two warps per
-// word, one lane per bit, so the 64 root lookups of a word run in parallel.
-__device__ __forceinline__ void apply_body(const JobDev &j, const double *U, int g, int bx, size_t lat, unsigned *s_sel) {
+// After the merge, every slab root whose piece was joined across a face is
+// re-pointed straight at its cluster's root; all such pieces touch a face, so
+// walking once from each face site reaches them.  Afterwards any site finds
+// its root in at most three loads (site -> slab root -> root).  Plain stores:
+// every value written is the final root of the same cluster.
+__device__ __forceinline__ void cc_compress_body(const JobDev &j, int D, int nslab, int r, size_t lat) {
+  const int L = j.L, S = L * L;
+  if (r >= nslab * S) return;
+  const int f = j.fd_S.div(r), xy = r - f * S;
+  int z, zm;
+  if (f == 0) {
+    if (j.bc != EA_PBC) return;
+    z = 0; zm = j.Lz - 1;
+  } else {
+    z = f * D; zm = z - 1;
+  }
+  uint32_t *lab = j.label + lat * j.V;
+  const uint32_t a = lab[xy + S * z], b = lab[xy + S * zm];
+  const uint32_t ra = cc_find(lab, a), rb = cc_find(lab, b);
+  if (ra != a) lab[a] = ra;
+  if (rb != b) lab[b] = rb;
+}
+
+// Offsets, in natural site index, of the 64 sites of a multispin word from
+// its bit-0 site: bit = bx + 4 by + 16 bz.
+__device__ __forceinline__ int word_bit_offset(const JobDev &j, int bit) {
+  return (bit & 3) * j.msc_l + ((bit >> 2) & 3) * j.msc_l * j.L + (bit >> 4) * j.msc_lz * j.L * j.L;
+}
+
+// Natural index of the bit-0 site of word (p, k).
+__device__ __forceinline__ int word_site0(const JobDev &j, int p, int k) {
+  const int hl = j.msc_l >> 1;
+  const int row = j.fd_hl.div(k), gz = j.fd_ml.div(row), gy = row - gz * j.msc_l;
+  const int gx = 2 * (k - row * hl) + ((gy + gz + p) & 1);
+  return gx + j.L * gy + j.L * j.L * gz;
+}
+
+// Selection and flip of one lattice in one CTA (HoudayerXEA.cu:54-75,358-374;
+// main.cu:776-832,938-991): bit i of s_bits is [U(root(i)) < 0.5], built in
+// natural order (coalesced label reads, one ballot per 32 sites); then each
+// word gathers its 64 bits from SMEM, q' = q xor sel, and s_r1 ^= q',
+// s_r2 ^= q'.  s_bits holds V/32 words, s_off 64.
+__device__ __forceinline__ void flip_body(const JobDev &j, const double *U, int g, size_t lat, uint32_t *s_bits,
+                                          int *s_off) {
+  const int t = threadIdx.x, nth = blockDim.x;
+  const int s = j.fd_nclust.div((uint32_t)lat), b = (int)lat - s * j.nclust;
+  const uint32_t *lab = j.label + lat * j.V;
+  const double *u = U + ((size_t)s * j.NB + b) * j.V;
+  if (t < 64) s_off[t] = word_bit_offset(j, t);
+  for (int base = 0; base < j.V; base += nth) {
+    const int site = base + t;
+    bool sel = false;
+    if (site < j.V) sel = __ldg(u + cc_find(lab, (uint32_t)site)) < 0.5;
+    const unsigned ball = __ballot_sync(0xffffffffu, sel);
+    if ((t & 31) == 0 && site < j.V) s_bits[site >> 5] = ball;
+  }
+  __syncthreads();
+  const int r1 = j.pairs[2 * g], r2 = j.pairs[2 * g + 1];
+  const int c1 = j.wctb[((size_t)s * j.NR + r1) * j.NB + b], c2 = j.wctb[((size_t)s * j.NR + r2) * j.NB + b];
+  const size_t wpc = (size_t)j.half * j.NR, wpp = wpc * j.NB;
+  const u64 *Q = j.Q + lat * 2 * j.half;
+  for (int w = t; w < 2 * j.half; w += nth) {
+    const int p = w >= j.half, k = w - p * j.half;
+    const int s0 = word_site0(j, p, k);
+    u64 mask = 0;
+#pragma unroll 16
+    for (int bit = 0; bit < 64; ++bit) {
+      const int site = s0 + s_off[bit];
+      mask |= (u64)((s_bits[site >> 5] >> (site & 31)) & 1u) << bit;
+    }
+    const u64 qn = Q[w] ^ mask;
+    u64 *base = j.spins + (size_t)s * 2 * wpp + (size_t)p * wpp + (size_t)k * j.NR;
+    base[(size_t)c1 * wpc + r1] ^= qn;
+    base[(size_t)c2 * wpc + r2] ^= qn;
+  }
+}
+
+// Cluster selection, natural order: bit i of sel[lat][i / 32] is
+// [U(root(i)) < 0.5] for site i (HoudayerXEA.cu:358-374).  Consecutive lanes
+// take consecutive sites, so the label reads are coalesced; the decisions of
+// a lattice (V / 8 bytes) then stay in cache for the word-order flip.
+__device__ __forceinline__ void select_body(const JobDev &j, const double *U, int site, size_t lat) {
+  const int s = j.fd_nclust.div((uint32_t)lat), b = (int)lat - s * j.nclust;
+  bool sel = false;
+  if (site < j.V) {
+    const uint32_t root = cc_find(j.label + lat * j.V, (uint32_t)site);
+    sel = __ldg(U + ((size_t)s * j.NB + b) * j.V + root) < 0.5;
+  }
+  const unsigned ball = __ballot_sync(0xffffffffu, sel);
+  if ((threadIdx.x & 31) == 0 && site < j.V) j.sel[lat * (j.V >> 5) + (site >> 5)] = ball;
+}
+
+// q' = q xor [selected] packed back into words, then s_r1 ^= q', s_r2 ^= q'
+// (HoudayerXEA.cu:54-75; main.cu:776-832,938-991).  Two warps per word, one
+// lane per bit.
+__device__ __forceinline__ void apply_body(const JobDev &j, int g, int bx, size_t lat, unsigned *s_sel) {
   const int t = threadIdx.x, wl = t >> 6, bit = t & 63;
   const int w = bx * 4 + wl;            // word of this lattice: parity * half + k
   const size_t i = lat * 2 * j.half + w;
@@ -539,8 +632,8 @@ __device__ __forceinline__ void apply_body(const JobDev &j, const double *U, int
     const int row = j.fd_hl.div(k), gz = j.fd_ml.div(row), gy = row - gz * j.msc_l;
     const int gx = 2 * (k - row * hl) + ((gy + gz + p) & 1);
     const int x = gx + (bit & 3) * j.msc_l, y = gy + ((bit >> 2) & 3) * j.msc_l, z = gz + (bit >> 4) * j.msc_lz;
-    const uint32_t root = cc_find(j.label + lat * j.V, (uint32_t)(x + j.L * y + j.L * j.L * z));
-    sel = __ldg(U + ((size_t)s * j.NB + b) * j.V + root) < 0.5;
+    const uint32_t site = (uint32_t)(x + j.L * y + j.L * j.L * z);
+    sel = (__ldg(j.sel + lat * (j.V >> 5) + (site >> 5)) >> (site & 31)) & 1u;
   }
   const unsigned ball = __ballot_sync(0xffffffffu, sel);
   if ((t & 31) == 0) s_sel[t >> 5] = ball;

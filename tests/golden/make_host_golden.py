@@ -38,6 +38,9 @@ CONFIGS = [
     ("L24_Lz192_NB32_OBC", 24, 192, 32, "OBC", 1, "T06_16_N32"),
 ]
 
+# temperature sets of the mixed-geometry (batched vs plain) and serving workloads
+EXTRA_LUTS = ["T07_16_N16", "T07_16_N24", "T07_16_N32", "T07_16_N8", "T07_16_N12"]
+
 
 def beta_set(name):
     """Temperatures uniform in [Tmin, Tmax]; betas written descending with 13 decimals."""
@@ -120,6 +123,10 @@ def main():
     if not os.path.isdir(REF):
         sys.exit("reference tree not found at %s" % REF)
     work = tempfile.mkdtemp(prefix="eagold_")
+    if sys.argv[1:] == ["luts"]:
+        for name in EXTRA_LUTS:
+            lut_fixture(name, beta_set(name), work)
+        return
     done_luts = {}
     for tag, L, Lz, NB, BC, nbits, bset in CONFIGS:
         if bset not in done_luts:
