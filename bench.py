@@ -223,6 +223,92 @@ def run_mixed(args, dev, torch, eagb, ns, copies):
             "l2": "inputs larger than L2 (spins ~0.3 GB, uniforms ~9 GB)"}
 
 
+# serving stream: Poisson arrivals of jobs with L in {8, 16} (the multiples of
+# 8 in 6..20), Lz/L in {1,2,4,8,16}, PBC/OBC, NT in {8,12,16,24,32} over
+# T in [0.7, 1.6], 8 samples, NR=4, a Houdayer move on the colder half every
+# 10 sweeps; sweeps log-uniform in 2^8..2^14 (the 2^14..2^20 range scaled by
+# 1/64 so that the stream lasts about half a minute), in bins of 20 sweeps
+SERVE_WORKLOAD = "poisson_L8-16_LzL1-16_PBC-OBC_NT8-32_NR4_ns8_houfr10_sweeps2^8-2^14"
+SERVE_NT, SERVE_NS, SERVE_NR = (8, 12, 16, 24, 32), 8, 4
+
+
+def serve_stream(njobs, seed=7):
+    rng = np.random.default_rng(seed)
+    jobs = []
+    for k in range(njobs):
+        L = int(rng.choice([8, 16]))
+        Lz = L * int(rng.choice([1, 2, 4, 8, 16]))
+        bc = int(rng.integers(0, 2))
+        nt = int(rng.choice(SERVE_NT))
+        sweeps = int(round(2.0 ** rng.uniform(8, 14)))
+        nbins = max(1, int(round(sweeps / 20.0)))
+        jobs.append((L, Lz, bc, nt, nbins))
+    return jobs
+
+
+def run_serve(args, dev, eagb, njobs=240, util=0.8):
+    """Continuous batching server under a Poisson stream of jobs: p50/p99
+    completion latency and spin-updates/ps of the completed work."""
+    import threading
+    stream = serve_stream(njobs)
+    luts = {nt: np.load(os.path.join(ROOT, "tests", "golden", "lut_T07_16_N%d.npz" % nt)) for nt in SERVE_NT}
+    su = [20 * nb * L * L * Lz * SERVE_NR * nt * SERVE_NS for (L, Lz, bc, nt, nb) in stream]
+    # arrival rate: the stream's work at ~0.6 spin-updates/ps, offered at `util`
+    mean_s = np.mean(su) / 0.6e12
+    rate = util / mean_s
+    rng = np.random.default_rng(11)
+    gaps = rng.exponential(1.0 / rate, size=njobs)
+    srv = eagb.Server(device=dev, nb_max=32, depth=2)
+    tickets = [None] * njobs
+    err = []
+
+    def producer():
+        t = time.perf_counter()
+        try:
+            for k, (L, Lz, bc, nt, nb) in enumerate(stream):
+                t += gaps[k]
+                d = time.perf_counter()
+                if t > d:
+                    time.sleep(t - d)
+                m = tuple((x ^ (0x9E3779B97F4A7C15 * (k + 1))) & 0xFFFFFFFFFFFFFFFF or 1 for x in MASTERS)
+                tickets[k] = srv.submit(L, Lz, luts[nt]["betas"], luts[nt]["cum"], SERVE_NS, SERVE_NR, bc, m, nb,
+                                        itmax=2, houfr=10, mesfr=1, ptfr=1, cluster=True, jobid=k & 0x3FFF)
+        except Exception as e:  # reported below
+            err.append(e)
+
+    th = threading.Thread(target=producer)
+    th.start()
+    # a finished job holds its bytes until released: release each as soon as
+    # it is done, whatever the order
+    done = [False] * njobs
+    t_limit = time.perf_counter() + 600.0
+    while not all(done) and time.perf_counter() < t_limit:
+        for k in range(njobs):
+            if done[k] or tickets[k] is None:
+                continue
+            st = srv.info(tickets[k])["state"]
+            if st == eagb.EA_JOB_DONE:
+                srv.release(tickets[k])
+                done[k] = True
+            elif st == eagb.EA_JOB_FAILED:
+                srv.wait(tickets[k], timeout=0.0)   # raises with the job's error
+        if not th.is_alive() and any(t is None for t in tickets):
+            break
+        time.sleep(0.0005)
+    th.join()
+    if err:
+        raise err[0]
+    st = srv.stats()
+    srv.close()
+    return {"workload": SERVE_WORKLOAD, "jobs": njobs, "arrival_rate_per_s": rate, "offered_load": util,
+            "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"], "max_ms": st["max_ms"],
+            "value": st["spin_updates"] / st["span_s"] / 1e12, "unit": "spin-updates/ps",
+            "span_s": st["span_s"], "completed": st["completed"], "failed": st["failed"],
+            "peak_running": st["peak_running"], "bins": st["bins"], "batch_changes": st["batch_changes"],
+            "hbm_budget": st["budget"], "hbm_peak": st["bytes_peak"], "gpu_busy_s": st["gpu_busy_s"],
+            "host_enqueue_s": st["enqueue_s"], "host_admit_s": st["admit_s"]}
+
+
 def run_ours(args, rank, world, local):
     import torch
     eagb = load_eagb()
@@ -347,6 +433,8 @@ def run_ours(args, rank, world, local):
     }
     if not args.no_mixed:
         line["batched"] = [run_mixed(args, dev, torch, eagb, 4, 8), run_mixed(args, dev, torch, eagb, 32, 1)]
+    if not args.no_serve:
+        line["serving"] = run_serve(args, dev, eagb)
     if not args.no_cpu:
         su, dt = cpu_sample(os.cpu_count() or 1, sweeps=20)
         line["cpu_baseline"] = {"value": su / dt / 1e12, "unit": "spin-updates/ps", "cores": os.cpu_count(),
@@ -366,6 +454,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the batched vs plain mixed-geometry leg")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving (Poisson stream) leg")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -20,7 +20,7 @@ CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-I" + os.path.join(ROOT, "include"), "-I" + CSRC, "-Xcompiler", "-fPIC"]
-SOURCES = ["kernels.cu", "batch.cu", "api.cu", "host.cpp", "noalloc.cu"]
+SOURCES = ["kernels.cu", "batch.cu", "api.cu", "host.cpp", "noalloc.cu", "serve.cpp"]
 
 
 def _compile(src):
@@ -46,7 +46,7 @@ def build(verbose=False):
     with ThreadPoolExecutor(len(SOURCES)) as ex:
         objs = list(ex.map(_compile, SOURCES))
     if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
-        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcurand"]
+        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcurand", "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed: %s\n%s" % (" ".join(cmd), r.stderr))

@@ -13,6 +13,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "eagb.h"
@@ -971,6 +972,13 @@ struct ea_batch {
   uint32_t *d_ctr = nullptr;
   std::vector<JobDev> up_jobs;  // JobDev array as last uploaded
   std::vector<uint32_t> up_pre;
+  // Uploads are stream-ordered copies from two pinned staging slots, so the
+  // work list can change between bins without waiting for the GPU; a slot is
+  // reused once the copy that read it has run (up_ev).
+  JobDev *h_jobs[2] = {};
+  uint32_t *h_pre[2] = {};
+  cudaEvent_t up_ev[2] = {};
+  int up_slot = 0;
   BatchDev bd{};
   cudaGraphExec_t cycle = nullptr;
   int cycle_ptfr = -1;
@@ -1042,13 +1050,20 @@ static int batch_upload(ea_batch *b) {
   const bool same = b->up_jobs.size() == hj.size() &&
                     !std::memcmp(b->up_jobs.data(), hj.data(), sizeof(JobDev) * n) && b->up_pre == hp;
   if (!same) {
-    // kernels of earlier bins may still read the arrays
-    CU(cudaStreamSynchronize(b->bs));
-    CU(cudaMemcpy(b->d_jobs, hj.data(), sizeof(JobDev) * n, cudaMemcpyHostToDevice));
-    CU(cudaMemcpy(b->d_pre, hp.data(), sizeof(uint32_t) * hp.size(), cudaMemcpyHostToDevice));
+    // kernels of earlier bins may still read the arrays: the copies are
+    // ordered after them on the batch stream
+    const int slot = b->up_slot;
+    b->up_slot ^= 1;
+    CU(cudaEventSynchronize(b->up_ev[slot]));
+    std::memcpy(b->h_jobs[slot], hj.data(), sizeof(JobDev) * n);
+    std::memcpy(b->h_pre[slot], hp.data(), sizeof(uint32_t) * hp.size());
+    CU(cudaMemcpyAsync(b->d_jobs, b->h_jobs[slot], sizeof(JobDev) * n, cudaMemcpyHostToDevice, b->bs));
+    CU(cudaMemcpyAsync(b->d_pre, b->h_pre[slot], sizeof(uint32_t) * hp.size(), cudaMemcpyHostToDevice, b->bs));
+    CU(cudaEventRecord(b->up_ev[slot], b->bs));
     b->up_jobs = hj;
     b->up_pre = hp;
   }
+  const BatchDev old_bd = b->bd;
   b->bd.jobs = b->d_jobs;
   b->bd.njobs = n;
   for (int k = 0; k < KB_COUNT; ++k) {
@@ -1063,6 +1078,11 @@ static int batch_upload(ea_batch *b) {
   const uint32_t chunk[KB_COUNT] = {1, 4, 1, 4, 4, 1, 4, 4, 1};
   for (int k = 0; k < KB_COUNT; ++k) b->bd.chunk[k] = chunk[k];
   if (b->bd.total[KB_SWEEP] >= 8u * 304u) b->bd.chunk[KB_SWEEP] = 2;
+  // the cycle graph holds the descriptor by value
+  if (std::memcmp(&old_bd, &b->bd, sizeof(BatchDev)) && b->cycle) {
+    cudaGraphExecDestroy(b->cycle);
+    b->cycle = nullptr;
+  }
   return EA_OK;
 }
 
@@ -1178,8 +1198,14 @@ int ea_batch_create(ea_ctx *const *jobs, int32_t njobs, int32_t tile, ea_batch *
   }
   cudaError_t e = cudaStreamCreateWithFlags(&b->bs, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
-  if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_jobs, sizeof(JobDev) * njobs);
-  if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_pre, sizeof(uint32_t) * KB_COUNT * (njobs + 1));
+  // room for the largest batch, so that ea_batch_set_jobs never reallocates
+  if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_jobs, sizeof(JobDev) * kBatchMaxJobs);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_pre, sizeof(uint32_t) * KB_COUNT * (kBatchMaxJobs + 1));
+  for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
+    e = cudaMallocHost((void **)&b->h_jobs[k], sizeof(JobDev) * kBatchMaxJobs);
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&b->h_pre[k], sizeof(uint32_t) * KB_COUNT * (kBatchMaxJobs + 1));
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->up_ev[k], cudaEventDisableTiming);
+  }
   if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_ctr, sizeof(uint32_t) * KB_COUNT);
   if (e == cudaSuccess) e = cudaMemset(b->d_ctr, 0, sizeof(uint32_t) * KB_COUNT);
   if (e == cudaSuccess && tile) e = batch_setup(b->NR, b->KT);
@@ -1200,6 +1226,11 @@ int ea_batch_destroy(ea_batch *b) {
   if (b->d_jobs) cudaFree(b->d_jobs);
   if (b->d_pre) cudaFree(b->d_pre);
   if (b->d_ctr) cudaFree(b->d_ctr);
+  for (int k = 0; k < 2; ++k) {
+    if (b->h_jobs[k]) cudaFreeHost(b->h_jobs[k]);
+    if (b->h_pre[k]) cudaFreeHost(b->h_pre[k]);
+    if (b->up_ev[k]) cudaEventDestroy(b->up_ev[k]);
+  }
   if (b->done) cudaEventDestroy(b->done);
   if (b->bs) cudaStreamDestroy(b->bs);
   delete b;
@@ -1210,6 +1241,34 @@ int ea_batch_tile(const ea_batch *b, int32_t *tile) {
   if (!b || !tile) return fail(EA_ERR_ARG, "null argument");
   *tile = b->KT;
   return EA_OK;
+}
+
+int ea_batch_set_jobs(ea_batch *b, ea_ctx *const *jobs, int32_t njobs) {
+  if (!b || !jobs || njobs < 1 || njobs > kBatchMaxJobs) return fail(EA_ERR_ARG, "1..%d jobs", kBatchMaxJobs);
+  std::vector<ea_ctx *> nj;
+  int nbmax = 0;
+  for (int i = 0; i < njobs; ++i) {
+    ea_ctx *c = jobs[i];
+    if (!c) return fail(EA_ERR_ARG, "null job %d", i);
+    if (std::find(nj.begin(), nj.end(), c) != nj.end()) return fail(EA_ERR_ARG, "job %d appears twice", i);
+    if (c->device != b->device || c->g.NR != b->NR)
+      return fail(EA_ERR_ARG, "the jobs of a batch share the device and the number of replicas");
+    if (c->g.NB > nbmax) nbmax = c->g.NB;
+    nj.push_back(c);
+  }
+  if (batch_sweep_smem(b->NR, b->KT, nbmax) > 227 * 1024 - 256)
+    return fail(EA_ERR_ARG, "NB=%d does not fit the batch's tile width %d", nbmax, b->KT);
+  CU(cudaSetDevice(b->device));
+  for (ea_ctx *c : nj) {
+    if (std::find(b->jobs.begin(), b->jobs.end(), c) != b->jobs.end()) continue;
+    const int rc = set_tile(c, b->KT);
+    if (rc) return rc;
+  }
+  std::stable_sort(nj.begin(), nj.end(),
+                   [](const ea_ctx *x, const ea_ctx *y) { return x->g.NB * x->g.ns > y->g.NB * y->g.ns; });
+  b->jobs = nj;
+  b->NBmax = nbmax;
+  return batch_upload(b);
 }
 
 // One tempering cycle for every job: ptfr sweeps (energy fused into the last
@@ -1284,9 +1343,11 @@ int ea_batch_run_bin(ea_batch *b, const ea_cadence *cad) {
     CU(cudaStreamWaitEvent(b->bs, b->done, 0));
   }
   // buffers that grow are reallocated only once the batch's earlier kernels ended
+  // (a job that joined the batch since has none yet, so it costs no wait)
   bool grow = false;
   for (ea_ctx *c : b->jobs)
-    grow = grow || maxit > c->hist_cap || (cad->cluster && norm_nclust(c->g, cad->nclust) > c->nclust_cap);
+    grow = grow || (c->hist && maxit > c->hist_cap) ||
+           (c->label && cad->cluster && norm_nclust(c->g, cad->nclust) > c->nclust_cap);
   if (grow) CU(cudaStreamSynchronize(b->bs));
   for (ea_ctx *c : b->jobs) {
     const Geometry &g = c->g;
@@ -1340,6 +1401,95 @@ int ea_batch_sync(ea_batch *b) {
 int ea_batch_stream(ea_batch *b, void **stream) {
   if (!b || !stream) return fail(EA_ERR_ARG, "null argument");
   *stream = (void *)b->bs;
+  return EA_OK;
+}
+
+int ea_init_run(ea_ctx *c, const uint64_t masters[4], const int32_t *list_samples, int64_t iter0, uint32_t jobid) {
+  if (check(c) || !masters) return fail(EA_ERR_ARG, "null argument");
+  const Geometry &g = c->g;
+  std::vector<uint64_t> sJ(g.ns), su(g.ns), sMC(g.NR);
+  int rc = ea_host_seeds(masters[0], masters[1], masters[2], masters[3], list_samples, g.ns, g.NR, sJ.data(),
+                         su.data(), sMC.data());
+  if (rc) return rc;
+  std::vector<ea_generators> gen(1);
+  std::vector<ea_hq> pt((size_t)g.ns * g.NR);
+  if ((rc = ea_host_generators(sMC.data(), list_samples, g.ns, g.NR, masters[3], gen.data(), pt.data()))) return rc;
+  if ((rc = ea_set_generators(c, gen.data(), pt.data()))) return rc;
+  ea_geom eg;
+  ea_get_geom(c, &eg);
+  // the samples' spins and couplings are independent host streams: built
+  // on up to 8 threads, then uploaded in sample order
+  const size_t n = g.words_per_parity(), nj = (size_t)12 * g.half;
+  std::vector<uint64_t> words((size_t)g.ns * (2 * n + nj));
+  std::vector<int> rcs(g.ns, EA_OK);
+  auto build = [&](int s) {
+    uint64_t *w = words.data() + (size_t)s * (2 * n + nj);
+    int32_t cnt = 0;
+    rcs[s] = ea_host_init_spins(&eg, su[s], w, w + n);
+    if (!rcs[s]) rcs[s] = ea_host_init_couplings(&eg, sJ[s], nullptr, w + 2 * n, &cnt);
+  };
+  const int nth = std::min(g.ns, 8);
+  std::vector<std::thread> pool;
+  for (int t = 0; t < nth; ++t)
+    pool.emplace_back([&, t] {
+      for (int s = t; s < g.ns; s += nth) build(s);
+    });
+  for (auto &t : pool) t.join();
+  for (int s = 0; s < g.ns; ++s) {
+    if (rcs[s]) return fail(rcs[s], "initial state of sample %d", s);
+    const uint64_t *w = words.data() + (size_t)s * (2 * n + nj);
+    if ((rc = ea_set_spins(c, s, w, w + n))) return rc;
+    if ((rc = ea_set_couplings(c, s, w + 2 * n))) return rc;
+  }
+  if ((rc = ea_set_permutations(c, nullptr))) return rc;
+  return ea_set_counter(c, iter0, jobid);
+}
+
+int ea_job_bytes(const ea_geom *gp, const ea_cadence *cad, const double *betas, uint64_t *bytes) {
+  Geometry g;
+  if (!gp || !bytes || !g.set(*gp)) return fail(EA_ERR_ARG, "geometry: L, Lz multiples of 8, 2<=NB<=255, 1<=nsamples<=32");
+  // each allocation rounded to the allocator's granule: 2 MiB pages for
+  // allocations of 1 MiB and more, 512 bytes below (small ones share pages)
+  uint64_t tot = 0;
+  auto add = [&](uint64_t n) {
+    n = std::max<uint64_t>(n, 1);
+    tot += n >= (1ull << 20) ? (n + (2ull << 20) - 1) & ~((2ull << 20) - 1) : (n + 511) & ~(uint64_t)511;
+  };
+  const uint64_t nsr = (uint64_t)g.ns * g.NR, NB = g.NB, half = g.half, V = g.V;
+  const int ktmin = g.NR == 8 ? 1 : g.NR == 4 ? 2 : 4;
+  add((uint64_t)g.ns * g.words_per_sample() * 8);            // spins
+  add((uint64_t)g.ns * 12 * half * 8);                       // couplings
+  add(12 * half * 4); add(2 * half);                         // neighbour table, flags
+  add(NB * 256 * 8); add(NB * 256 * 2);                      // thresholds, pre-search
+  add(nsr * NB); add(nsr * NB);                              // permutations
+  add(g.NR * 16); add(g.NR * 4); add(g.NR * sizeof(ea_hq)); add(g.NR * sizeof(ea_xoshiro)); add(8);
+  add(2 * ((half + ktmin - 1) / ktmin) * nsr * NB * 4);      // energy partials (two tile widths at most)
+  add(nsr * NB * 4); add(nsr * sizeof(ea_hq)); add(NB * 8); add(NB * 4);
+  for (int k = 0; k < 3; ++k) add(nsr * (NB - 1) * 8);       // tempering statistics
+  add(8); add(sizeof(ea_hq)); add(16); add(nsr * NB * 8);    // inexact, random_c, pairs, averages
+  uint64_t nexp = 0;                                         // glibc exp table
+  if (betas) {
+    std::vector<double> tab;
+    std::vector<int32_t> off;
+    pt_exp_table(betas, g.NB, tab, off);
+    nexp = tab.size();
+  } else {
+    nexp = (NB - 1) * 25001;  // temperature steps down to 1e-3
+  }
+  add(nexp * 8);
+  int maxit = 1;
+  if (cad && cad->itmax > 0) {
+    int frec;
+    trw(cad->itmax, &frec, &maxit);
+  }
+  add(nsr * maxit * NB);                                     // temperature history
+  if (cad && cad->cluster) {
+    const uint64_t ncl = (uint64_t)norm_nclust(g, cad->nclust);
+    for (int k = 0; k < 4; ++k) add(V * NB * g.ns * 8);      // uniforms: two sets of two groups
+    add(V * ncl * g.ns * 4); add(V / 32 * ncl * g.ns * 4); add(2 * half * ncl * g.ns * 8);
+    tot += 4ull << 20;                                       // cuRAND generator state
+  }
+  *bytes = tot + (4ull << 20);                               // streams, events, pages of the small allocations
   return EA_OK;
 }
 

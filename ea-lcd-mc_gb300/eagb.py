@@ -40,6 +40,31 @@ class Cadence(C.Structure):
     _fields_ = [(n, C.c_int32) for n in ("itmax", "houfr", "mesfr", "ptfr", "cluster", "nclust")]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("device", C.c_int32), ("max_jobs", C.c_int32), ("depth", C.c_int32), ("tile", C.c_int32),
+                ("nb_max", C.c_int32), ("reserved", C.c_int32), ("hbm_budget", C.c_uint64)]
+
+
+class Request(C.Structure):
+    _fields_ = [("geom", Geom), ("betas", C.c_void_p), ("cum", C.c_void_p), ("masters", C.c_uint64 * 4),
+                ("cad", Cadence), ("nbins", C.c_int32), ("jobid", C.c_uint32), ("iter0", C.c_int64)]
+
+
+class JobInfo(C.Structure):
+    _fields_ = [("state", C.c_int32), ("bins_done", C.c_int32), ("t_submit", C.c_double), ("t_admit", C.c_double),
+                ("t_done", C.c_double), ("bytes", C.c_uint64), ("spin_updates", C.c_double)]
+
+
+class ServeStats(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in ("submitted", "admitted", "completed", "failed", "queued", "running",
+                                          "bins", "batch_changes", "peak_running")] + \
+               [(n, C.c_double) for n in ("p50_ms", "p99_ms", "mean_ms", "max_ms", "spin_updates", "span_s")] + \
+               [(n, C.c_uint64) for n in ("budget", "bytes_in_use", "bytes_peak")] + \
+               [(n, C.c_double) for n in ("gpu_busy_s", "enqueue_s", "admit_s")]
+
+
+EA_JOB_QUEUED, EA_JOB_RUNNING, EA_JOB_DONE, EA_JOB_FAILED, EA_JOB_RELEASED = range(5)
+
 _lib = None
 
 
@@ -315,3 +340,84 @@ def new_job(L, Lz, betas, cum, nsamples=1, NR=8, bc=EA_OBC, masters=(1, 2, 3, 4)
     job.set_permutations(None)
     job.set_counter(iter0, jobid)
     return job
+
+
+def job_bytes(g, cad=None, betas=None):
+    """Device bytes a job holds (ea_job_bytes): what admission charges."""
+    out = C.c_uint64()
+    b = None if betas is None else np.ascontiguousarray(betas, np.float64)
+    _ck(lib().ea_job_bytes(C.byref(g), None if cad is None else C.byref(cad), None if b is None else P(b),
+                           C.byref(out)))
+    return out.value
+
+
+def init_run(job, masters, iter0=0, jobid=0, list_samples=None):
+    """ea_init_run: a new run on an existing job, set up in the library."""
+    m = (C.c_uint64 * 4)(*[int(x) for x in masters])
+    ls = None if list_samples is None else np.ascontiguousarray(list_samples, np.int32)
+    _ck(lib().ea_init_run(job.ctx, m, None if ls is None else P(ls), C.c_int64(iter0), C.c_uint32(jobid)))
+
+
+class ServedJob(Job):
+    """View of a finished server job (the context stays owned by the server)."""
+
+    def __init__(self, g, ctx):
+        self.g = g
+        self.half, self.V = sizes(g)
+        self.ctx = ctx
+
+    def close(self):
+        self.ctx = None
+
+    def __del__(self):
+        pass
+
+
+class Server:
+    """Continuous batching server (ea_server_*): submit jobs at any time, wait
+    for each, read its results, release it."""
+
+    def __init__(self, device=0, max_jobs=0, depth=0, tile=0, nb_max=0, hbm_budget=0):
+        cfg = ServerConfig(device, max_jobs, depth, tile, nb_max, 0, hbm_budget)
+        self.s = C.c_void_p()
+        _ck(lib().ea_server_create(C.byref(cfg), C.byref(self.s)))
+        self._geoms = {}
+        self._keep = {}
+
+    def submit(self, L, Lz, betas, cum, nsamples, NR, bc, masters, nbins, itmax, houfr, mesfr, ptfr,
+               cluster=True, nclust=0, jobid=0, iter0=0):
+        betas = np.ascontiguousarray(betas, np.float64)
+        cum = np.ascontiguousarray(cum, np.uint64)
+        g = geom(L, Lz, len(betas), NR, nsamples, bc)
+        r = Request(g, betas.ctypes.data, cum.ctypes.data, (C.c_uint64 * 4)(*[int(x) for x in masters]),
+                    Cadence(itmax, houfr, mesfr, ptfr, int(cluster), nclust), nbins, jobid, iter0)
+        t = C.c_int64()
+        _ck(lib().ea_server_submit(self.s, C.byref(r), C.byref(t)))
+        self._geoms[t.value] = g
+        return t.value
+
+    def wait(self, ticket, timeout=-1.0):
+        ctx = C.c_void_p()
+        _ck(lib().ea_server_wait(self.s, C.c_int64(ticket), C.c_double(timeout), C.byref(ctx)))
+        return ServedJob(self._geoms[ticket], ctx)
+
+    def info(self, ticket):
+        i = JobInfo()
+        _ck(lib().ea_server_info(self.s, C.c_int64(ticket), C.byref(i)))
+        return {f: getattr(i, f) for f, _ in JobInfo._fields_}
+
+    def release(self, ticket):
+        _ck(lib().ea_server_release(self.s, C.c_int64(ticket)))
+
+    def stats(self):
+        st = ServeStats()
+        _ck(lib().ea_server_stats(self.s, C.byref(st)))
+        return {f: getattr(st, f) for f, _ in ServeStats._fields_}
+
+    def drain(self):
+        _ck(lib().ea_server_drain(self.s))
+
+    def close(self):
+        if self.s:
+            _ck(lib().ea_server_destroy(self.s))
+            self.s = None

@@ -224,6 +224,12 @@ typedef struct ea_batch ea_batch;
 int ea_batch_create(ea_ctx *const *jobs, int32_t njobs, int32_t tile, ea_batch **out);
 int ea_batch_destroy(ea_batch *b);
 int ea_batch_tile(const ea_batch *b, int32_t *tile);
+/* Replaces the batch's jobs between bins (continuous batching): jobs that
+ * stay keep their state, new ones join with the batch's tile width, jobs that
+ * leave are ordered after the bins they took part in.  The new work list is
+ * uploaded in stream order, so the call does not wait for bins in flight.
+ * Fails with EA_ERR_ARG if the largest NB no longer fits the tile width. */
+int ea_batch_set_jobs(ea_batch *b, ea_ctx *const *jobs, int32_t njobs);
 /* One bin of the cadence for every job, enqueued without a host
  * synchronisation; read each job's results with ea_bin_results. */
 int ea_batch_run_bin(ea_batch *b, const ea_cadence *cad);
@@ -241,6 +247,92 @@ int ea_check_exact(ea_ctx *ctx);
 enum { EA_K_SWEEP = 0, EA_K_PT = 1, EA_K_CLUSTER = 2, EA_K_ENERGY = 3, EA_K_RNG = 4, EA_K_COUNT = 5 };
 int ea_profile(ea_ctx *ctx, int32_t on);
 int ea_kernel_time(ea_ctx *ctx, int32_t kind, int64_t *launches, double *total_ms);
+
+/* A new run (flag 1 of the reference) on an existing context, as Init() does
+ * (ini.c:32-101, 316-383, 465-730, 763-781): seeds from the four master seeds
+ * (seed_J, seed_u, seed_MC, seed_cluster), generators, initial spins,
+ * couplings, identity permutations, then the Philox counter and job id
+ * (main.cu:59-62).  list_samples may be NULL (samples 0..nsamples-1). */
+int ea_init_run(ea_ctx *ctx, const uint64_t masters[4], const int32_t *list_samples, int64_t iter0, uint32_t jobid);
+/* Upper bound of the device bytes a job of geometry g holds once it has run
+ * bins of cadence cad (NULL: no bin yet) -- what admission by an HBM budget
+ * charges for it.  betas (may be NULL) sizes the tempering exp table exactly. */
+int ea_job_bytes(const ea_geom *g, const ea_cadence *cad, const double *betas, uint64_t *bytes);
+
+/* ---- serving: continuous batching of simulation jobs -------------------------
+ * A server owns one device and a worker thread.  Submitted jobs wait in a
+ * queue until their device bytes (ea_job_bytes) fit the HBM budget and a slot
+ * is free; admitted jobs are created and initialised as new runs
+ * (ea_init_run), join the batch of their replica count and cadence, and are
+ * advanced one bin per step by the batched kernels, interleaved with every
+ * other running job; a job leaves its batch after its last bin.  Up to
+ * `depth` bins per batch are in flight, and the job list of a batch changes
+ * between bins without draining the GPU.  Each job's words, energies, swaps
+ * and uniforms equal those of the same job run alone by ea_run_bin.  Latency
+ * is submission to completion as the worker observes it (host clock).  A
+ * finished job's context stays readable (ea_get_spins, ea_bin_results, ...)
+ * until ea_server_release.  No reference counterpart: the reference runs one
+ * job per process. */
+typedef struct ea_server ea_server;
+typedef struct {
+  int32_t device;
+  int32_t max_jobs;      /* jobs admitted at once (<= 0: 1024) */
+  int32_t depth;         /* bins in flight per batch (<= 0: 2) */
+  int32_t tile;          /* sweep tile width of the batches (0: the widest that fits nb_max) */
+  int32_t nb_max;        /* largest accepted NB (<= 0: 64) */
+  int32_t reserved;
+  uint64_t hbm_budget;   /* device bytes the jobs may hold (0: 90 % of the free memory at creation) */
+} ea_server_config;
+
+typedef struct {
+  ea_geom geom;
+  const double *betas;   /* [nbetas], copied */
+  const uint64_t *cum;   /* [nbetas][256], copied */
+  uint64_t masters[4];   /* seed_J, seed_u, seed_MC, seed_cluster */
+  ea_cadence cad;        /* one bin */
+  int32_t nbins;         /* bins to run (>= 1) */
+  uint32_t jobid;        /* 14-bit Philox job id */
+  int64_t iter0;         /* initial half-sweep counter */
+} ea_request;
+
+enum { EA_JOB_QUEUED = 0, EA_JOB_RUNNING = 1, EA_JOB_DONE = 2, EA_JOB_FAILED = 3, EA_JOB_RELEASED = 4 };
+typedef struct {
+  int32_t state;
+  int32_t bins_done;
+  double t_submit, t_admit, t_done;  /* seconds since the server's creation (-1: not yet) */
+  uint64_t bytes;                    /* charged against the budget */
+  double spin_updates;
+} ea_job_info;
+
+typedef struct {
+  int64_t submitted, admitted, completed, failed, queued, running;
+  int64_t bins, batch_changes, peak_running;
+  double p50_ms, p99_ms, mean_ms, max_ms;  /* completion latency of the completed jobs */
+  double spin_updates;                     /* of the completed jobs */
+  double span_s;                           /* first submission to last completion */
+  uint64_t budget, bytes_in_use, bytes_peak;
+  double gpu_busy_s;  /* sum of the bins' device durations (CUDA events) */
+  double enqueue_s;   /* worker time spent enqueueing bins (batch changes included) */
+  double admit_s;     /* worker time spent creating and initialising admitted jobs */
+} ea_serve_stats;
+
+int ea_server_create(const ea_server_config *cfg, ea_server **out);
+/* Queues a job; returns EA_ERR_ARG for a request that can never run (bad
+ * geometry, NB above nb_max, bytes above the budget). */
+int ea_server_submit(ea_server *s, const ea_request *r, int64_t *ticket);
+/* Waits until the job is done or failed (timeout_s < 0: no limit); job (may be
+ * NULL) receives its context, still owned by the server.  EA_ERR_STATE on
+ * timeout; the job's own error code if it failed. */
+int ea_server_wait(ea_server *s, int64_t ticket, double timeout_s, ea_ctx **job);
+int ea_server_info(ea_server *s, int64_t ticket, ea_job_info *info);
+/* Frees a finished job's device memory (asynchronously; the budget is
+ * credited once it is freed). */
+int ea_server_release(ea_server *s, int64_t ticket);
+int ea_server_stats(ea_server *s, ea_serve_stats *st);
+/* Waits until every submitted job has finished. */
+int ea_server_drain(ea_server *s);
+/* Cancels queued jobs, waits for the running ones' bins and frees everything. */
+int ea_server_destroy(ea_server *s);
 
 /* cuRAND XORWOW uniforms (device generator) for a seed/offset, copied to host.
  * Used to check the device generator against the host one. */
