@@ -1,0 +1,783 @@
+// sp.cu -- kernels of the sample-packed layout (64 samples per word) and its
+// C ABI (ea_sp_*).  See sp.cuh for the layout.
+#include <cuda.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "host.hpp"
+#include "kernels_dev.cuh"
+#include "sp.cuh"
+
+namespace eagb {
+
+void set_last_error(const char *msg);  // api.cu
+
+// ---------------------------------------------------------------------------
+// Philox counters of a colour pass: the reference's fill_bits step per
+// replica (fill_bits.h:47-68) with the pass counter in place of the
+// half-sweep counter (its parity bit = the counter's lowest bit, as for
+// half-sweeps), so every pass of every sweep has its own counters.
+// ---------------------------------------------------------------------------
+__global__ void k_sp_fill(const __grid_constant__ SpDev d) {
+  JobDev j{};
+  j.NR = d.NR; j.xo = d.xo; j.prc = d.prc; j.ctr = d.ctr; j.iter = d.iter; j.jobid = d.jobid;
+  const int parity = (int)(*d.iter & 1);
+  fill_bits_body(j, parity);
+}
+
+// ---------------------------------------------------------------------------
+// One colour pass.  A CTA owns kt sites of the colour: it stages every
+// temperature's thresholds in SMEM, draws the three random words of each
+// (slot, site, replica) once -- shared by the nw sample words, as the
+// reference shares them across samples (main.cu:1430) -- and updates all
+// (word, site, replica, slot) words of its tile in memory order, so that
+// consecutive lanes touch consecutive words of a site.  The Philox thread
+// index of (slot b, site i, replica r) is (b*V + i)*NR + r.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(512) k_sp_pass(const __grid_constant__ SpDev d, int off, int n) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int NB = d.NB, NR = d.NR, kt = d.kt, V = d.V;
+  u64 *s_cum = reinterpret_cast<u64 *>(smem);
+  uint16_t *s_pre = reinterpret_cast<uint16_t *>(s_cum + NB * 256);
+  u64 *s_rnd = reinterpret_cast<u64 *>(s_pre + NB * 256);
+  int *s_nb = reinterpret_cast<int *>(s_rnd + 3 * NB * kt * NR);  // [kt][7]: site, 6 neighbours
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const int k0 = blockIdx.x * kt;
+  {
+    const uint4 *cs = reinterpret_cast<const uint4 *>(d.cum);
+    uint4 *cd = reinterpret_cast<uint4 *>(s_cum);
+    for (int i = tid; i < NB * 128; i += nth) cd[i] = cs[i];
+    const uint4 *ps = reinterpret_cast<const uint4 *>(d.pre);
+    uint4 *pd = reinterpret_cast<uint4 *>(s_pre);
+    for (int i = tid; i < NB * 32; i += nth) pd[i] = ps[i];
+  }
+  for (int i = tid; i < kt * 7; i += nth) {
+    const int kk = i / 7, f = i % 7, k = k0 + kk;
+    int v = -1;
+    if (k < n) {
+      const int site = d.col_sites[off + k];
+      v = f == 0 ? site : d.nb[(size_t)site * 6 + f - 1];
+    }
+    s_nb[i] = v;
+  }
+  __syncthreads();
+  const int plane = NB * kt * NR;
+  for (int t = tid; t < plane; t += nth) {
+    const int r = t % NR, kk = (t / NR) % kt, b = t / (NR * kt);
+    if (k0 + kk >= n) continue;
+    const int site = s_nb[kk * 7];
+    const uint32_t tp = (uint32_t)(((size_t)b * V + site) * NR + r);
+    const uint4 c = d.ctr[r];
+    const uint32_t key = d.keys[r];
+    const u64 *cum = s_cum + b * 256;
+    const uint16_t *pre = s_pre + b * 256;
+    uint32_t w[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) w[q] = rnd_word(c.x + q, c.y, c.z + tp, c.w, key, tp, cum, pre);
+    s_rnd[t] = ((u64)w[0] << 32) | w[1];
+    s_rnd[plane + t] = ((u64)w[2] << 32) | w[3];
+    s_rnd[2 * plane + t] = ((u64)w[4] << 32) | w[5];
+  }
+  __syncthreads();
+  const int G = NR * NB;
+  const size_t wps = (size_t)V * G;  // words per sample word
+  const int total = kt * d.nw * G;
+  for (int i = tid; i < total; i += nth) {
+    const int b = i % NB, r = (i / NB) % NR, kk = (i / G) % kt, w = i / (G * kt);
+    if (k0 + kk >= n) continue;
+    const int *sn = s_nb + kk * 7;
+    const int site = sn[0];
+    u64 *Sw = d.S + (size_t)w * wps + r * NB + b;
+    const u64 *Jp = d.J + ((size_t)w * V + site) * 6;
+    const u64 sv = Sw[(size_t)site * G];
+    u64 f[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) f[q] = sv ^ __ldg(Jp + q) ^ Sw[(size_t)sn[q + 1] * G];
+    const int o = (b * kt + kk) * NR + r;
+    Sw[(size_t)site * G] = sv ^ flip_mask(f, s_rnd[o], s_rnd[plane + o], s_rnd[2 * plane + o]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Energy: per (word, sample, replica, slot) the number of unsatisfied
+// half-edges U2 (each bond counted from both ends), so E = 3V - U2
+// (main.cu:1379).  A thread owns one (replica, slot) column of a word over a
+// chunk of sites and counts the unsatisfied slots of each sample with
+// bit-sliced counters (one bit plane per power of two, all 64 samples at
+// once), then adds its per-sample totals to U2.
+// ---------------------------------------------------------------------------
+constexpr int kSpChunk = 256;  // sites per thread: 6 * 256 < 2^11
+constexpr int kSpPlanes = 11;
+
+__global__ void __launch_bounds__(256) k_sp_energy(const __grid_constant__ SpDev d) {
+  const int G = d.NR * d.NB, V = d.V;
+  const int nchunk = (V + kSpChunk - 1) / kSpChunk;
+  const long long col = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // over nw * nchunk * G
+  if (col >= (long long)d.nw * nchunk * G) return;
+  const int rb = (int)(col % G), ch = (int)((col / G) % nchunk), w = (int)(col / ((long long)G * nchunk));
+  const u64 *Sw = d.S + (size_t)w * V * G + rb;
+  const u64 *Jw = d.J + (size_t)w * V * 6;
+  u64 P[kSpPlanes];
+#pragma unroll
+  for (int p = 0; p < kSpPlanes; ++p) P[p] = 0;
+  const int i0 = ch * kSpChunk, i1 = min(V, i0 + kSpChunk);
+  for (int i = i0; i < i1; ++i) {
+    const u64 sv = Sw[(size_t)i * G];
+    const int *nb = d.nb + (size_t)i * 6;
+    u64 f[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) f[q] = sv ^ __ldg(Jw + (size_t)i * 6 + q) ^ Sw[(size_t)__ldg(nb + q) * G];
+    // six bits -> a 3-bit count per sample (two full adders and a merge)
+    const u64 x1 = f[0] ^ f[1] ^ f[2], y1 = (f[0] & f[1]) | (f[2] & (f[0] ^ f[1]));
+    const u64 x2 = f[3] ^ f[4] ^ f[5], y2 = (f[3] & f[4]) | (f[5] & (f[3] ^ f[4]));
+    const u64 z0 = x1 ^ x2, c0 = x1 & x2;
+    const u64 z1 = y1 ^ y2 ^ c0, z2 = (y1 & y2) | (c0 & (y1 ^ y2));
+    // add z0 + 2 z1 + 4 z2 to the counter planes
+    u64 c = P[0] & z0;
+    P[0] ^= z0;
+    u64 s = P[1] ^ z1 ^ c;
+    c = (P[1] & z1) | (c & (P[1] ^ z1));
+    P[1] = s;
+    s = P[2] ^ z2 ^ c;
+    c = (P[2] & z2) | (c & (P[2] ^ z2));
+    P[2] = s;
+#pragma unroll
+    for (int p = 3; p < kSpPlanes; ++p) {
+      const u64 t = P[p] & c;
+      P[p] ^= c;
+      c = t;
+    }
+  }
+  int32_t *U = d.U2 + (size_t)w * 64 * G + rb;
+  for (int lane = 0; lane < 64; ++lane) {
+    int cnt = 0;
+#pragma unroll
+    for (int p = 0; p < kSpPlanes; ++p) cnt |= (int)((P[p] >> lane) & 1ull) << p;
+    if (cnt) atomicAdd(U + (size_t)lane * G, cnt);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Tempering: one thread per (word, sample, replica) chain; the rule of
+// upd.c:3-48 over the slot pairs in order (pt = -(b[i+1]-b[i]) * dE in FP64,
+// accept when pt >= 0 or FNORM * u < exp(pt), exp from the host's libm table;
+// beyond the table exp(pt) < 2^-72 and only u = 0 accepts).  The 64-bit
+// uniform u of (step, pair, chain) is Philox4x32-10 keyed by the job's
+// tempering seed -- the reference draws it from a per-chain Parisi-Rapuano
+// generator; sample-packed jobs have 64 chains per word, so a counter-based
+// draw replaces the 2 KB of state per chain.  A warp holds 32 samples of one
+// (word, replica): the accepted swaps of pair i form the lane mask M[i].
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(64) k_sp_pt(const __grid_constant__ SpDev d) {
+  const int NB = d.NB, NR = d.NR, G = NR * NB;
+  const int wr = blockIdx.x, w = wr / NR, r = wr % NR, lane = threadIdx.x;
+  const int nt = 3 * d.V;
+  const size_t o = ((size_t)w * 64 + lane) * G + (size_t)r * NB;
+  const unsigned long long step = *d.ptstep;
+  const uint32_t chain = (uint32_t)(((size_t)w * 64 + lane) * NR + r);
+  const double FNORM = 5.4210108624275218e-20;
+  int E[64];
+  uint8_t pm[64];
+  for (int b = 0; b < NB; ++b) {
+    E[b] = nt - d.U2[o + b];
+    pm[b] = d.perm[o + b];
+  }
+  uint32_t *acc = d.acc + ((size_t)w * 64 + lane) * NR * (NB - 1) + (size_t)r * (NB - 1);
+  uint32_t *Mh = reinterpret_cast<uint32_t *>(d.M + ((size_t)w * NR + r) * (NB - 1));
+  for (int i = 0; i < NB - 1; ++i) {
+    const int dE = E[i + 1] - E[i];
+    const double pt = __dmul_rn(-__dsub_rn(d.betas[i + 1], d.betas[i]), (double)dE);
+    uint32_t v0 = (uint32_t)step, v1 = (uint32_t)(step >> 32), v2 = (uint32_t)i, v3 = chain;
+    philox10(v0, v1, v2, v3, (uint32_t)d.pt_seed, (uint32_t)(d.pt_seed >> 32));
+    const u64 u = ((u64)v0 << 32) | v1;
+    bool change;
+    if (pt >= 0.0) {
+      change = true;
+    } else {
+      const int base = d.expoff[i], m = (-dE) >> 1, nx = d.expoff[i + 1] - base;
+      change = (m >= 1 && m <= nx) ? __dmul_rn(FNORM, __ull2double_rn(u)) < d.exptab[base + m - 1] : u == 0;
+    }
+    if (change) {
+      const int te = E[i]; E[i] = E[i + 1]; E[i + 1] = te;
+      const uint8_t tp = pm[i]; pm[i] = pm[i + 1]; pm[i + 1] = tp;
+      acc[i] += 1u;
+    }
+    const unsigned mask = __ballot_sync(0xffffffffu, change);
+    if ((lane & 31) == 0) Mh[2 * i + (lane >> 5)] = mask;
+  }
+  for (int b = 0; b < NB; ++b) {
+    d.E[o + b] = E[b];
+    d.perm[o + b] = pm[b];
+  }
+}
+
+// The accepted swaps of the last tempering step, applied to the words in
+// pair order: slot i exchanges the masked samples with slot i+1, and is final
+// after that (one carry word per thread).  Thread per (word, site, replica).
+__global__ void k_sp_permute(const __grid_constant__ SpDev d) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t == 0) *d.ptstep += 1ull;
+  const int NB = d.NB, NR = d.NR;
+  if (t >= (long long)d.nw * d.V * NR) return;
+  const int r = (int)(t % NR), w = (int)(t / ((long long)NR * d.V));
+  u64 *p = d.S + (size_t)t * NB;
+  const u64 *M = d.M + ((size_t)w * NR + r) * (NB - 1);
+  u64 cur = p[0];
+  for (int i = 0; i < NB - 1; ++i) {
+    const u64 m = __ldg(M + i);
+    u64 nxt = p[i + 1];
+    const u64 x = (cur ^ nxt) & m;
+    p[i] = cur ^ x;
+    cur = nxt ^ x;
+  }
+  p[NB - 1] = cur;
+}
+
+__global__ void k_sp_measure(const __grid_constant__ SpDev d) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < (long long)d.nw * 64 * d.NR * d.NB) d.avgE[i] += (double)d.E[i];
+}
+
+// ---------------------------------------------------------------------------
+// Exact enumeration: for every sample of every word, the number of spin
+// configurations at each energy E = 3V - U2 among the 2^(V-1) with spin 0 up
+// (E is even under the global flip, so the full counts are twice these; the
+// averages do not change).  Block row y = sample.  A thread walks 2^12
+// configurations in Gray-code order from a prefix of the higher spins:
+// flipping spin k changes U2 by 2 (6 - 2 n_k), n_k = unsatisfied slots at k.
+// Counts go to a per-block SMEM histogram, then to the 64-bit global one.
+// ---------------------------------------------------------------------------
+constexpr int kDosLow = 12;
+
+__global__ void __launch_bounds__(256) k_sp_dos(const __grid_constant__ SpDev d, int nprefix_bits) {
+  __shared__ uint32_t h[6 * 32 + 1];
+  const int V = d.V, nbins = 6 * V + 1;
+  const int sample = blockIdx.y, w = sample / 64, lane = sample % 64;
+  __shared__ int s_nb[32 * 6];
+  __shared__ uint8_t s_j[32 * 6];
+  for (int i = threadIdx.x; i < nbins; i += blockDim.x) h[i] = 0;
+  for (int i = threadIdx.x; i < V * 6; i += blockDim.x) {
+    s_nb[i] = d.nb[i];
+    s_j[i] = (uint8_t)((d.J[(size_t)w * V * 6 + i] >> lane) & 1ull);
+  }
+  __syncthreads();
+  const int nlow = min(kDosLow, V - 1);
+  const uint64_t prefix = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (prefix < (1ull << nprefix_bits)) {
+    // configuration bits: spin 0 up (bit 0 = 0), spins 1..nlow by Gray code,
+    // the rest from the prefix
+    uint32_t s = (uint32_t)(prefix << (nlow + 1));
+    auto unsat = [&](int k) {
+      int n = 0;
+      const int sk = (s >> k) & 1;
+#pragma unroll
+      for (int q = 0; q < 6; ++q) n += sk ^ (int)((s >> s_nb[k * 6 + q]) & 1u) ^ s_j[k * 6 + q];
+      return n;
+    };
+    int U2 = 0;
+    for (int k = 0; k < V; ++k) U2 += unsat(k);
+    atomicAdd(&h[3 * V - U2 + 3 * V], 1u);
+    for (uint32_t g = 1; g < (1u << nlow); ++g) {
+      const int k = __ffs(g);  // Gray step g flips spin 1 + (trailing zeros of g)
+      const int nk = unsat(k);
+      U2 += 2 * (6 - 2 * nk);
+      s ^= 1u << k;
+      atomicAdd(&h[3 * V - U2 + 3 * V], 1u);
+    }
+  }
+  __syncthreads();
+  unsigned long long *out = d.dos + (size_t)sample * nbins;
+  for (int i = threadIdx.x; i < nbins; i += blockDim.x)
+    if (h[i]) atomicAdd(out + i, (unsigned long long)h[i]);
+}
+
+// <E>(beta) of each sample from its density of states, in FP64: weights
+// g(E) exp(beta (E - Emax)) over the bins.
+__global__ void k_sp_exact(const __grid_constant__ SpDev d, const double *betas, int nbeta, double *meanE) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int V = d.V, nbins = 6 * V + 1;
+  if (t >= d.nw * 64 * nbeta) return;
+  const int sample = t / nbeta, k = t % nbeta;
+  const unsigned long long *g = d.dos + (size_t)sample * nbins;
+  int emax = -3 * V;
+  for (int i = 0; i < nbins; ++i)
+    if (g[i]) emax = i - 3 * V;
+  double Z = 0, ZE = 0;
+  for (int i = 0; i < nbins; ++i) {
+    if (!g[i]) continue;
+    const int E = i - 3 * V;
+    const double wgt = (double)g[i] * exp(betas[k] * (double)(E - emax));
+    Z += wgt;
+    ZE += wgt * (double)E;
+  }
+  meanE[t] = ZE / Z;
+}
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+size_t sp_sweep_smem(int NB, int NR, int kt) {
+  return (size_t)NB * 256 * 10 + (size_t)3 * NB * kt * NR * 8 + (size_t)kt * 7 * 4;
+}
+
+// Tile width: the widest power of two up to 64 whose SMEM fits and that still
+// gives two tiles per SM, else the widest that fits.
+int sp_kt(int NB, int NR, int nsites_colour) {
+  int best = 0;
+  for (int kt = 64; kt >= 1; kt >>= 1) {
+    if (sp_sweep_smem(NB, NR, kt) > 227 * 1024) continue;
+    if (!best) best = kt;
+    if ((nsites_colour + kt - 1) / kt >= 2 * 152) return kt;
+  }
+  return best;
+}
+
+cudaError_t sp_setup() {
+  return cudaFuncSetAttribute(k_sp_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+}
+
+cudaError_t sp_launch_pass(const SpDev &d, int colour, int off, int n, cudaStream_t st) {
+  k_sp_fill<<<1, 64, 0, st>>>(d);
+  (void)colour;
+  if (n > 0) {
+    const int grid = (n + d.kt - 1) / d.kt;
+    k_sp_pass<<<grid, 512, sp_sweep_smem(d.NB, d.NR, d.kt), st>>>(d, off, n);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t sp_launch_energy(const SpDev &d, cudaStream_t st) {
+  const int G = d.NR * d.NB;
+  cudaError_t e = cudaMemsetAsync(d.U2, 0, sizeof(int32_t) * (size_t)d.nw * 64 * G, st);
+  if (e != cudaSuccess) return e;
+  const long long n = (long long)d.nw * ((d.V + kSpChunk - 1) / kSpChunk) * G;
+  k_sp_energy<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d);
+  return cudaGetLastError();
+}
+
+cudaError_t sp_launch_pt(const SpDev &d, cudaStream_t st) {
+  k_sp_pt<<<d.nw * d.NR, 64, 0, st>>>(d);
+  return cudaGetLastError();
+}
+
+cudaError_t sp_launch_permute(const SpDev &d, cudaStream_t st) {
+  const long long n = (long long)d.nw * d.V * d.NR;
+  k_sp_permute<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d);
+  return cudaGetLastError();
+}
+
+cudaError_t sp_launch_measure(const SpDev &d, cudaStream_t st) {
+  const long long n = (long long)d.nw * 64 * d.NR * d.NB;
+  k_sp_measure<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d);
+  return cudaGetLastError();
+}
+
+cudaError_t sp_launch_dos(const SpDev &d, cudaStream_t st) {
+  const int nlow = std::min(kDosLow, d.V - 1);
+  const int npre = d.V - 1 - nlow;
+  const unsigned long long nthreads = 1ull << npre;
+  const dim3 grid((unsigned)((nthreads + 255) / 256), (unsigned)(d.nw * 64));
+  k_sp_dos<<<grid, 256, 0, st>>>(d, npre);
+  return cudaGetLastError();
+}
+
+cudaError_t sp_launch_exact(const SpDev &d, const double *betas, int nbeta, double *meanE, cudaStream_t st) {
+  const int n = d.nw * 64 * nbeta;
+  k_sp_exact<<<(n + 127) / 128, 128, 0, st>>>(d, betas, nbeta, meanE);
+  return cudaGetLastError();
+}
+
+}  // namespace eagb
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+using namespace eagb;
+
+namespace {
+int spfail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  set_last_error(buf);
+  return code;
+}
+#define SCU(call)                                                                             \
+  do {                                                                                        \
+    cudaError_t e_ = (call);                                                                  \
+    if (e_ != cudaSuccess) return spfail(EA_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+}  // namespace
+
+struct ea_sp {
+  ea_sp_geom geom{};
+  SpGraph g;
+  int device = 0;
+  cudaStream_t st = nullptr;
+  SpDev d{};
+  std::vector<void *> owned;
+  std::vector<int32_t> expoff;
+  double *exptab = nullptr;
+  bool have_temps = false;
+};
+
+namespace {
+template <class T>
+int sp_own(ea_sp *c, T *&p, size_t n) {
+  cudaError_t e = cudaMalloc((void **)&p, sizeof(T) * (n ? n : 1));
+  if (e != cudaSuccess) return spfail(EA_ERR_NOMEM, "cudaMalloc(%zu bytes): %s", sizeof(T) * n, cudaGetErrorString(e));
+  c->owned.push_back((void *)p);
+  cudaMemsetAsync(p, 0, sizeof(T) * (n ? n : 1), c->st);
+  return EA_OK;
+}
+
+bool geom_ok(const ea_sp_geom *g) {
+  return g && g->nbetas >= 2 && g->nbetas <= 64 && g->nrep >= 1 && g->nrep <= 64 && g->nwords >= 1 &&
+         g->nwords <= (1 << 20);
+}
+}  // namespace
+
+extern "C" {
+
+int ea_sp_graph(int32_t L, int32_t Lz, int32_t bc, int32_t *nb, int32_t *mate, uint8_t *colour, int32_t *ncol) {
+  SpGraph g;
+  if (!sp_graph(L, Lz, bc, g)) return spfail(EA_ERR_ARG, "tube %d x %d x %d (bc %d) not supported", L, L, Lz, bc);
+  if (nb) std::memcpy(nb, g.nb.data(), g.nb.size() * 4);
+  if (mate) std::memcpy(mate, g.mate.data(), g.mate.size() * 4);
+  if (colour) std::memcpy(colour, g.colour.data(), g.colour.size());
+  if (ncol) *ncol = g.ncol;
+  return EA_OK;
+}
+
+int ea_sp_host_init(const ea_sp_geom *gp, uint64_t seed_J, uint64_t seed_u, uint64_t *J, uint64_t *S) {
+  SpGraph g;
+  if (!geom_ok(gp) || !sp_graph(gp->L, gp->Lz, gp->bc, g)) return spfail(EA_ERR_ARG, "bad sample-packed geometry");
+  if (J) sp_couplings(g, gp->nwords, seed_J, J);
+  if (S) sp_spins(g, gp->nwords, gp->nrep, gp->nbetas, seed_u, S);
+  return EA_OK;
+}
+
+int ea_sp_create(const ea_sp_geom *gp, int32_t device, ea_sp **out) {
+  if (!gp || !out) return spfail(EA_ERR_ARG, "null argument");
+  if (!geom_ok(gp)) return spfail(EA_ERR_ARG, "2 <= nbetas <= 64, 1 <= nrep <= 64, nwords >= 1");
+  ea_sp *c = new ea_sp();
+  c->geom = *gp;
+  if (!sp_graph(gp->L, gp->Lz, gp->bc, c->g)) {
+    delete c;
+    return spfail(EA_ERR_ARG, "tube %d x %d x %d (bc %d) not supported", gp->L, gp->L, gp->Lz, gp->bc);
+  }
+  const SpGraph &g = c->g;
+  SpDev &d = c->d;
+  d.L = g.L; d.Lz = g.Lz; d.V = g.V; d.bc = g.bc; d.NB = gp->nbetas; d.NR = gp->nrep; d.nw = gp->nwords;
+  d.ncol = g.ncol;
+  int maxc = 0;
+  for (int k = 0; k < g.ncol; ++k) maxc = std::max(maxc, g.col_off[k + 1] - g.col_off[k]);
+  d.kt = sp_kt(d.NB, d.NR, maxc);
+  if (!d.kt) { delete c; return spfail(EA_ERR_ARG, "NB=%d x NR=%d does not fit in shared memory", d.NB, d.NR); }
+  c->device = device;
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = sp_setup();
+  if (e != cudaSuccess) { delete c; return spfail(EA_ERR_CUDA, "set-up: %s", cudaGetErrorString(e)); }
+  const size_t G = (size_t)d.NR * d.NB, V = g.V, nw = d.nw;
+  int rc;
+#define SOWN(p, n) if ((rc = sp_own(c, p, n)) != EA_OK) { ea_sp_destroy(c); return rc; }
+  { int32_t *p; SOWN(p, V * 6); d.nb = p; }
+  { int32_t *p; SOWN(p, V); d.col_sites = p; }
+  SOWN(d.S, nw * V * G);
+  { unsigned long long *p; SOWN(p, nw * V * 6); d.J = p; }
+  { unsigned long long *p; SOWN(p, (size_t)d.NB * 256); d.cum = p; }
+  { uint16_t *p; SOWN(p, (size_t)d.NB * 256); d.pre = p; }
+  SOWN(d.ctr, (size_t)d.NR);
+  { uint32_t *p; SOWN(p, (size_t)d.NR); d.keys = p; }
+  SOWN(d.prc, (size_t)d.NR);
+  SOWN(d.xo, (size_t)d.NR);
+  SOWN(d.iter, 1);
+  SOWN(d.U2, nw * 64 * G);
+  SOWN(d.E, nw * 64 * G);
+  SOWN(d.perm, nw * 64 * G);
+  SOWN(d.acc, nw * 64 * d.NR * (d.NB - 1));
+  SOWN(d.M, nw * d.NR * (d.NB - 1));
+  { double *p; SOWN(p, (size_t)d.NB); d.betas = p; }
+  { int32_t *p; SOWN(p, (size_t)d.NB); d.expoff = p; }
+  SOWN(d.ptstep, 1);
+  SOWN(d.avgE, nw * 64 * G);
+#undef SOWN
+  SCU(cudaMemcpyAsync((void *)d.nb, g.nb.data(), V * 6 * 4, cudaMemcpyHostToDevice, c->st));
+  SCU(cudaMemcpyAsync((void *)d.col_sites, g.col_sites.data(), V * 4, cudaMemcpyHostToDevice, c->st));
+  // identity slot -> configuration map
+  std::vector<uint8_t> perm(nw * 64 * G);
+  for (size_t i = 0; i < perm.size(); ++i) perm[i] = (uint8_t)(i % d.NB);
+  SCU(cudaMemcpyAsync(d.perm, perm.data(), perm.size(), cudaMemcpyHostToDevice, c->st));
+  SCU(cudaStreamSynchronize(c->st));
+  *out = c;
+  return EA_OK;
+}
+
+int ea_sp_destroy(ea_sp *c) {
+  if (!c) return EA_OK;
+  cudaSetDevice(c->device);
+  if (c->st) cudaStreamSynchronize(c->st);
+  for (void *p : c->owned) cudaFree(p);
+  if (c->exptab) cudaFree(c->exptab);
+  if (c->d.dos) cudaFree(c->d.dos);
+  if (c->st) cudaStreamDestroy(c->st);
+  delete c;
+  return EA_OK;
+}
+
+int ea_sp_info(const ea_sp *c, int32_t *ncol, int32_t *tile) {
+  if (!c) return spfail(EA_ERR_ARG, "null job");
+  if (ncol) *ncol = c->d.ncol;
+  if (tile) *tile = c->d.kt;
+  return EA_OK;
+}
+
+int ea_sp_stream(ea_sp *c, void **stream) {
+  if (!c || !stream) return spfail(EA_ERR_ARG, "null argument");
+  *stream = (void *)c->st;
+  return EA_OK;
+}
+
+int ea_sp_sync(ea_sp *c) {
+  if (!c) return spfail(EA_ERR_ARG, "null job");
+  SCU(cudaSetDevice(c->device));
+  SCU(cudaStreamSynchronize(c->st));
+  return EA_OK;
+}
+
+int ea_sp_set_temperatures(ea_sp *c, const double *betas, const uint64_t *cum) {
+  if (!c || !betas || !cum) return spfail(EA_ERR_ARG, "null argument");
+  const int NB = c->d.NB;
+  for (int i = 0; i + 1 < NB; ++i)
+    if (betas[i] < betas[i + 1]) return spfail(EA_ERR_ARG, "betas must be sorted from largest to smallest");
+  std::vector<uint16_t> pre((size_t)NB * 256);
+  for (int b = 0; b < NB; ++b) {
+    if (cum[(size_t)b * 256 + 255] != ~0ULL) return spfail(EA_ERR_ARG, "threshold 255 of beta %d is not 2^64-1", b);
+    presearch8(cum + (size_t)b * 256, pre.data() + (size_t)b * 256);
+  }
+  std::vector<double> tab;
+  pt_exp_table(betas, NB, tab, c->expoff);
+  SCU(cudaSetDevice(c->device));
+  SCU(cudaStreamSynchronize(c->st));
+  if (c->exptab) cudaFree(c->exptab);
+  c->exptab = nullptr;
+  SCU(cudaMalloc((void **)&c->exptab, sizeof(double) * std::max<size_t>(1, tab.size())));
+  SCU(cudaMemcpyAsync(c->exptab, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice, c->st));
+  SCU(cudaMemcpyAsync((void *)c->d.cum, cum, sizeof(uint64_t) * 256 * NB, cudaMemcpyHostToDevice, c->st));
+  SCU(cudaMemcpyAsync((void *)c->d.pre, pre.data(), pre.size() * 2, cudaMemcpyHostToDevice, c->st));
+  SCU(cudaMemcpyAsync((void *)c->d.betas, betas, sizeof(double) * NB, cudaMemcpyHostToDevice, c->st));
+  SCU(cudaMemcpyAsync((void *)c->d.expoff, c->expoff.data(), sizeof(int32_t) * NB, cudaMemcpyHostToDevice, c->st));
+  SCU(cudaStreamSynchronize(c->st));
+  c->d.exptab = c->exptab;
+  c->have_temps = true;
+  return EA_OK;
+}
+
+int ea_sp_set_generators(ea_sp *c, const ea_generators *gen, uint64_t pt_seed) {
+  if (!c || !gen) return spfail(EA_ERR_ARG, "null argument");
+  const int NR = c->d.NR;
+  SCU(cudaSetDevice(c->device));
+  SCU(cudaMemcpyAsync(c->d.prc, gen->prc, sizeof(ea_hq) * NR, cudaMemcpyHostToDevice, c->st));
+  SCU(cudaMemcpyAsync(c->d.xo, gen->xo, sizeof(ea_xoshiro) * NR, cudaMemcpyHostToDevice, c->st));
+  SCU(cudaMemcpyAsync((void *)c->d.keys, gen->keys, sizeof(uint32_t) * NR, cudaMemcpyHostToDevice, c->st));
+  SCU(cudaStreamSynchronize(c->st));
+  c->d.pt_seed = pt_seed;
+  return EA_OK;
+}
+
+int ea_sp_get_generators(ea_sp *c, ea_generators *gen) {
+  if (!c || !gen) return spfail(EA_ERR_ARG, "null argument");
+  const int NR = c->d.NR;
+  std::memset(gen, 0, sizeof(*gen));
+  SCU(cudaSetDevice(c->device));
+  SCU(cudaMemcpyAsync(gen->prc, c->d.prc, sizeof(ea_hq) * NR, cudaMemcpyDeviceToHost, c->st));
+  SCU(cudaMemcpyAsync(gen->xo, c->d.xo, sizeof(ea_xoshiro) * NR, cudaMemcpyDeviceToHost, c->st));
+  SCU(cudaMemcpyAsync(gen->keys, c->d.keys, sizeof(uint32_t) * NR, cudaMemcpyDeviceToHost, c->st));
+  SCU(cudaStreamSynchronize(c->st));
+  return EA_OK;
+}
+
+int ea_sp_init(ea_sp *c, const uint64_t seeds[4], uint32_t jobid) {
+  if (!c || !seeds) return spfail(EA_ERR_ARG, "null argument");
+  const SpDev &d = c->d;
+  const size_t G = (size_t)d.NR * d.NB;
+  std::vector<uint64_t> J((size_t)d.nw * d.V * 6), S((size_t)d.nw * d.V * G);
+  sp_couplings(c->g, d.nw, seeds[0], J.data());
+  sp_spins(c->g, d.nw, d.NR, d.NB, seeds[1], S.data());
+  // Metropolis generators per replica as Init_Random seeds them
+  // (random_generator.cu:94-158, 203-241), from seed_MC
+  std::vector<uint64_t> sMC(d.NR);
+  seeds_from_one(seeds[2], sMC.data(), d.NR);
+  std::vector<ea_generators> gen(1);
+  std::memset(gen.data(), 0, sizeof(ea_generators));
+  for (int r = 0; r < d.NR; ++r) init_generators(sMC[r], gen[0].prc[r], gen[0].xo[r], gen[0].keys[r]);
+  int rc = ea_sp_set_couplings(c, J.data());
+  if (!rc) rc = ea_sp_set_spins(c, S.data());
+  if (!rc) rc = ea_sp_set_generators(c, gen.data(), seeds[3]);
+  if (!rc) rc = ea_sp_set_counter(c, 0, 0, jobid);
+  return rc;
+}
+
+int ea_sp_set_spins(ea_sp *c, const uint64_t *S) {
+  if (!c || !S) return spfail(EA_ERR_ARG, "null argument");
+  SCU(cudaSetDevice(c->device));
+  SCU(cudaMemcpyAsync(c->d.S, S, (size_t)c->d.nw * c->d.V * c->d.NR * c->d.NB * 8, cudaMemcpyHostToDevice, c->st));
+  SCU(cudaStreamSynchronize(c->st));
+  return EA_OK;
+}
+
+int ea_sp_get_spins(ea_sp *c, uint64_t *S) {
+  if (!c || !S) return spfail(EA_ERR_ARG, "null argument");
+  SCU(cudaSetDevice(c->device));
+  SCU(cudaMemcpyAsync(S, c->d.S, (size_t)c->d.nw * c->d.V * c->d.NR * c->d.NB * 8, cudaMemcpyDeviceToHost, c->st));
+  SCU(cudaStreamSynchronize(c->st));
+  return EA_OK;
+}
+
+int ea_sp_set_couplings(ea_sp *c, const uint64_t *J) {
+  if (!c || !J) return spfail(EA_ERR_ARG, "null argument");
+  SCU(cudaSetDevice(c->device));
+  SCU(cudaMemcpyAsync((void *)c->d.J, J, (size_t)c->d.nw * c->d.V * 6 * 8, cudaMemcpyHostToDevice, c->st));
+  SCU(cudaStreamSynchronize(c->st));
+  return EA_OK;
+}
+
+int ea_sp_set_counter(ea_sp *c, int64_t iter, uint64_t ptstep, uint32_t jobid) {
+  if (!c || jobid >= (1u << 14)) return spfail(EA_ERR_ARG, "job id < 2^14");
+  SCU(cudaSetDevice(c->device));
+  c->d.jobid = jobid;
+  SCU(cudaMemcpyAsync(c->d.iter, &iter, 8, cudaMemcpyHostToDevice, c->st));
+  SCU(cudaMemcpyAsync(c->d.ptstep, &ptstep, 8, cudaMemcpyHostToDevice, c->st));
+  SCU(cudaStreamSynchronize(c->st));
+  return EA_OK;
+}
+
+int ea_sp_get_counter(ea_sp *c, int64_t *iter, uint64_t *ptstep) {
+  if (!c) return spfail(EA_ERR_ARG, "null job");
+  SCU(cudaSetDevice(c->device));
+  int64_t it = 0;
+  uint64_t ps = 0;
+  SCU(cudaMemcpyAsync(&it, c->d.iter, 8, cudaMemcpyDeviceToHost, c->st));
+  SCU(cudaMemcpyAsync(&ps, c->d.ptstep, 8, cudaMemcpyDeviceToHost, c->st));
+  SCU(cudaStreamSynchronize(c->st));
+  if (iter) *iter = it;
+  if (ptstep) *ptstep = ps;
+  return EA_OK;
+}
+
+static int sp_sweeps(ea_sp *c, int n) {
+  const SpGraph &g = c->g;
+  for (int s = 0; s < n; ++s)
+    for (int k = 0; k < g.ncol; ++k)
+      SCU(sp_launch_pass(c->d, k, g.col_off[k], g.col_off[k + 1] - g.col_off[k], c->st));
+  return EA_OK;
+}
+
+int ea_sp_sweeps(ea_sp *c, int32_t n) {
+  if (!c || n < 0) return spfail(EA_ERR_ARG, "bad arguments");
+  if (!c->have_temps) return spfail(EA_ERR_STATE, "temperatures not set");
+  SCU(cudaSetDevice(c->device));
+  return sp_sweeps(c, n);
+}
+
+int ea_sp_energy(ea_sp *c, int32_t *U2) {
+  if (!c) return spfail(EA_ERR_ARG, "null job");
+  SCU(cudaSetDevice(c->device));
+  SCU(sp_launch_energy(c->d, c->st));
+  if (U2) {
+    SCU(cudaMemcpyAsync(U2, c->d.U2, sizeof(int32_t) * (size_t)c->d.nw * 64 * c->d.NR * c->d.NB,
+                        cudaMemcpyDeviceToHost, c->st));
+    SCU(cudaStreamSynchronize(c->st));
+  }
+  return EA_OK;
+}
+
+static int sp_pt(ea_sp *c) {
+  SCU(sp_launch_energy(c->d, c->st));
+  SCU(sp_launch_pt(c->d, c->st));
+  SCU(sp_launch_permute(c->d, c->st));
+  return EA_OK;
+}
+
+int ea_sp_parallel_tempering(ea_sp *c) {
+  if (!c) return spfail(EA_ERR_ARG, "null job");
+  if (!c->have_temps) return spfail(EA_ERR_STATE, "temperatures not set");
+  SCU(cudaSetDevice(c->device));
+  return sp_pt(c);
+}
+
+int ea_sp_get_tempering(ea_sp *c, int32_t *E, uint8_t *perm, uint32_t *acc, uint64_t *masks) {
+  if (!c) return spfail(EA_ERR_ARG, "null job");
+  const SpDev &d = c->d;
+  const size_t n = (size_t)d.nw * 64 * d.NR * d.NB;
+  SCU(cudaSetDevice(c->device));
+  if (E) SCU(cudaMemcpyAsync(E, d.E, n * 4, cudaMemcpyDeviceToHost, c->st));
+  if (perm) SCU(cudaMemcpyAsync(perm, d.perm, n, cudaMemcpyDeviceToHost, c->st));
+  if (acc) SCU(cudaMemcpyAsync(acc, d.acc, (size_t)d.nw * 64 * d.NR * (d.NB - 1) * 4, cudaMemcpyDeviceToHost, c->st));
+  if (masks) SCU(cudaMemcpyAsync(masks, d.M, (size_t)d.nw * d.NR * (d.NB - 1) * 8, cudaMemcpyDeviceToHost, c->st));
+  SCU(cudaStreamSynchronize(c->st));
+  return EA_OK;
+}
+
+int ea_sp_run(ea_sp *c, int32_t ncycles, int32_t ptfr, int32_t mesfr, double *avgE, int32_t *nmeas) {
+  if (!c || ncycles < 0 || ptfr < 1 || mesfr < 1) return spfail(EA_ERR_ARG, "bad cadence");
+  if (!c->have_temps) return spfail(EA_ERR_STATE, "temperatures not set");
+  SCU(cudaSetDevice(c->device));
+  const SpDev &d = c->d;
+  const size_t n = (size_t)d.nw * 64 * d.NR * d.NB;
+  SCU(cudaMemsetAsync(d.avgE, 0, n * 8, c->st));
+  int m = 0;
+  for (int cy = 0; cy < ncycles; ++cy) {
+    int rc = sp_sweeps(c, ptfr);
+    if (!rc) rc = sp_pt(c);
+    if (rc) return rc;
+    if ((cy + 1) % mesfr == 0) {
+      SCU(sp_launch_measure(d, c->st));
+      ++m;
+    }
+  }
+  if (nmeas) *nmeas = m;
+  if (avgE) {
+    SCU(cudaMemcpyAsync(avgE, d.avgE, n * 8, cudaMemcpyDeviceToHost, c->st));
+    SCU(cudaStreamSynchronize(c->st));
+  }
+  return EA_OK;
+}
+
+int ea_sp_exact(ea_sp *c, const double *betas, int32_t nbeta, uint64_t *dos, double *meanE) {
+  if (!c) return spfail(EA_ERR_ARG, "null job");
+  const SpDev &d0 = c->d;
+  if (d0.V > 32) return spfail(EA_ERR_ARG, "exact enumeration needs V <= 32 sites (V = %d)", d0.V);
+  if (meanE && (!betas || nbeta < 1)) return spfail(EA_ERR_ARG, "betas");
+  SCU(cudaSetDevice(c->device));
+  const size_t nbins = 6 * (size_t)d0.V + 1, ns = (size_t)d0.nw * 64;
+  if (!c->d.dos) SCU(cudaMalloc((void **)&c->d.dos, ns * nbins * 8));
+  const SpDev &d = c->d;
+  SCU(cudaMemsetAsync(d.dos, 0, ns * nbins * 8, c->st));
+  SCU(sp_launch_dos(d, c->st));
+  if (dos) SCU(cudaMemcpyAsync(dos, d.dos, ns * nbins * 8, cudaMemcpyDeviceToHost, c->st));
+  if (meanE) {
+    double *db = nullptr, *dm = nullptr;
+    SCU(cudaMalloc((void **)&db, sizeof(double) * nbeta));
+    SCU(cudaMalloc((void **)&dm, sizeof(double) * ns * nbeta));
+    SCU(cudaMemcpyAsync(db, betas, sizeof(double) * nbeta, cudaMemcpyHostToDevice, c->st));
+    SCU(sp_launch_exact(d, db, nbeta, dm, c->st));
+    SCU(cudaMemcpyAsync(meanE, dm, sizeof(double) * ns * nbeta, cudaMemcpyDeviceToHost, c->st));
+    SCU(cudaStreamSynchronize(c->st));
+    cudaFree(db);
+    cudaFree(dm);
+  }
+  SCU(cudaStreamSynchronize(c->st));
+  return EA_OK;
+}
+
+}  // extern "C"

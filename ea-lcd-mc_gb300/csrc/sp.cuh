@@ -1,0 +1,79 @@
+// sp.cuh -- sample-packed layout: 64 disorder samples per 64-bit word (bit b =
+// sample b of the word), for tubes of any L >= 2 and Lz >= 2 and any number of
+// replicas.  The reference's multispin layout packs 64 sub-blocks of ONE
+// sample per word and so needs L and Lz multiples of 8 (PROGRAM/include/
+// header.h:41-47); here every word of a site holds the same site of 64
+// samples, so the lattice is a plain site list with a neighbour table and a
+// proper colouring (2 colours for bipartite tubes, more otherwise).
+//
+// The update arithmetic is the reference's: Philox4x32-10 random words turned
+// into heat-bath bits through the temperature's 64-bit thresholds
+// (main.cu:994-1150), the bit-sliced local field and flip mask
+// (main.cu:1474-1506), 6 bond slots per site with the reference's fake bond
+// on the open z planes (ini.c:551-641, main.cu:1460-1472), E = 3V - 2 x
+// unsatisfied bonds (main.cu:1379) and the tempering rule of upd.c:3-48.
+// Each temperature slot has a fixed beta; tempering swaps move the
+// configurations of the accepted samples between slots (lane masks).
+#pragma once
+#include <cstdint>
+#include <vector>
+#include <cuda_runtime.h>
+#include "eagb.h"
+
+namespace eagb {
+
+// Lattice graph of the sample-packed layout (host).
+struct SpGraph {
+  int L = 0, Lz = 0, bc = 0, V = 0, ncol = 0;
+  std::vector<int32_t> nb;         // [V][6] neighbour site of each bond slot (+x,+y,+z,-x,-y,-z)
+  std::vector<int32_t> mate;       // [V][6] half-edge index p*6+slot' of the other end
+  std::vector<uint8_t> colour;     // [V]
+  std::vector<int32_t> col_off;    // [ncol+1]
+  std::vector<int32_t> col_sites;  // [V] sites grouped by colour, ascending
+};
+bool sp_graph(int L, int Lz, int bc, SpGraph &g);
+void sp_couplings(const SpGraph &g, int nwords, uint64_t seed_J, uint64_t *J);
+void sp_spins(const SpGraph &g, int nwords, int NR, int NB, uint64_t seed_u, uint64_t *S);
+
+// Device view of a sample-packed job (kernel parameter).
+struct SpDev {
+  int L, Lz, V, bc, NB, NR, nw, ncol, kt;
+  const int32_t *nb;                 // [V][6]
+  const int32_t *col_sites;          // [V]
+  unsigned long long *S;             // [nw][V][NR][NB] spin words
+  const unsigned long long *J;       // [nw][V][6] coupling words
+  const unsigned long long *cum;     // [NB][256] thresholds
+  const uint16_t *pre;               // [NB][256] 8-bit pre-search
+  uint4 *ctr;                        // [NR] Philox counters of the current pass
+  const uint32_t *keys;              // [NR]
+  ea_hq *prc;                        // [NR]
+  ea_xoshiro *xo;                    // [NR]
+  long long *iter;                   // colour-pass counter
+  uint32_t jobid;
+  int32_t *U2;                       // [nw][64][NR][NB] unsatisfied half-edges (twice the bonds)
+  int32_t *E;                        // [nw][64][NR][NB] energy of the configuration at each slot
+  uint8_t *perm;                     // [nw][64][NR][NB] replica-local id of the configuration at each slot
+  uint32_t *acc;                     // [nw][64][NR][NB-1] accepted swaps
+  unsigned long long *M;             // [nw][NR][NB-1] lanes that swapped in the last tempering step
+  const double *betas;               // [NB] descending
+  const double *exptab;              // host-libm exp of the tempering exponents
+  const int32_t *expoff;             // [NB]
+  unsigned long long *ptstep;        // tempering steps so far
+  unsigned long long pt_seed;
+  double *avgE;                      // [nw][64][NR][NB]
+  // exact enumeration
+  unsigned long long *dos;           // [nw][64][6V+1] states per energy (E = -3V..3V)
+};
+
+int sp_kt(int NB, int NR, int nsites_colour);
+size_t sp_sweep_smem(int NB, int NR, int kt);
+cudaError_t sp_setup();
+cudaError_t sp_launch_pass(const SpDev &d, int colour, int off, int n, cudaStream_t st);
+cudaError_t sp_launch_energy(const SpDev &d, cudaStream_t st);
+cudaError_t sp_launch_pt(const SpDev &d, cudaStream_t st);
+cudaError_t sp_launch_permute(const SpDev &d, cudaStream_t st);
+cudaError_t sp_launch_measure(const SpDev &d, cudaStream_t st);
+cudaError_t sp_launch_dos(const SpDev &d, cudaStream_t st);
+cudaError_t sp_launch_exact(const SpDev &d, const double *betas, int nbeta, double *meanE, cudaStream_t st);
+
+}  // namespace eagb

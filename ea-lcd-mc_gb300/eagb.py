@@ -421,3 +421,126 @@ class Server:
         if self.s:
             _ck(lib().ea_server_destroy(self.s))
             self.s = None
+
+
+# ---------------------------------------------------------------------------
+# Sample-packed layout (ea_sp_*): 64 samples per word, any L >= 2, Lz >= 2
+# ---------------------------------------------------------------------------
+class SpGeom(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in ("L", "Lz", "nbetas", "nrep", "nwords", "bc")]
+
+
+def sp_graph(L, Lz, bc):
+    """Bond graph: nb [V,6], mate [V,6], colour [V], ncol."""
+    V = L * L * Lz
+    nb = np.zeros((V, 6), np.int32)
+    mate = np.zeros((V, 6), np.int32)
+    col = np.zeros(V, np.uint8)
+    n = C.c_int32()
+    _ck(lib().ea_sp_graph(L, Lz, bc, P(nb), P(mate), P(col), C.byref(n)))
+    return nb, mate, col, n.value
+
+
+def sp_host_init(g, seed_J, seed_u):
+    V = g.L * g.L * g.Lz
+    J = np.zeros((g.nwords, V, 6), np.uint64)
+    S = np.zeros((g.nwords, V, g.nrep, g.nbetas), np.uint64)
+    _ck(lib().ea_sp_host_init(C.byref(g), C.c_uint64(seed_J), C.c_uint64(seed_u), P(J), P(S)))
+    return J, S
+
+
+class SpJob:
+    """A sample-packed job (ea_sp): 64 * nwords samples of an L x L x Lz tube."""
+
+    def __init__(self, L, Lz, betas, cum, nrep=2, nwords=1, bc=EA_PBC, seeds=(1, 2, 3, 4), jobid=0, device=0):
+        betas = np.ascontiguousarray(betas, np.float64)
+        self.g = SpGeom(L, Lz, len(betas), nrep, nwords, bc)
+        self.V = L * L * Lz
+        self.betas = betas
+        self.h = C.c_void_p()
+        _ck(lib().ea_sp_create(C.byref(self.g), device, C.byref(self.h)))
+        _ck(lib().ea_sp_set_temperatures(self.h, P(betas), P(np.ascontiguousarray(cum, np.uint64))))
+        sd = (C.c_uint64 * 4)(*[int(x) for x in seeds])
+        _ck(lib().ea_sp_init(self.h, sd, C.c_uint32(jobid)))
+
+    def close(self):
+        if self.h:
+            _ck(lib().ea_sp_destroy(self.h))
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self):
+        nc, kt = C.c_int32(), C.c_int32()
+        _ck(lib().ea_sp_info(self.h, C.byref(nc), C.byref(kt)))
+        return nc.value, kt.value
+
+    def stream(self):
+        v = C.c_void_p()
+        _ck(lib().ea_sp_stream(self.h, C.byref(v)))
+        return v.value
+
+    def sync(self):
+        _ck(lib().ea_sp_sync(self.h))
+
+    def get_spins(self):
+        S = np.zeros((self.g.nwords, self.V, self.g.nrep, self.g.nbetas), np.uint64)
+        _ck(lib().ea_sp_get_spins(self.h, P(S)))
+        return S
+
+    def set_spins(self, S):
+        _ck(lib().ea_sp_set_spins(self.h, P(np.ascontiguousarray(S, np.uint64))))
+
+    def get_generators(self):
+        gen = Generators()
+        _ck(lib().ea_sp_get_generators(self.h, C.byref(gen)))
+        return gen
+
+    def counter(self):
+        it, ps = C.c_int64(), C.c_uint64()
+        _ck(lib().ea_sp_get_counter(self.h, C.byref(it), C.byref(ps)))
+        return it.value, ps.value
+
+    def sweeps(self, n):
+        _ck(lib().ea_sp_sweeps(self.h, n))
+
+    def energy(self):
+        U2 = np.zeros((self.g.nwords, 64, self.g.nrep, self.g.nbetas), np.int32)
+        _ck(lib().ea_sp_energy(self.h, P(U2)))
+        return U2
+
+    def parallel_tempering(self):
+        _ck(lib().ea_sp_parallel_tempering(self.h))
+
+    def tempering(self):
+        nw, NR, NB = self.g.nwords, self.g.nrep, self.g.nbetas
+        E = np.zeros((nw, 64, NR, NB), np.int32)
+        perm = np.zeros((nw, 64, NR, NB), np.uint8)
+        acc = np.zeros((nw, 64, NR, NB - 1), np.uint32)
+        M = np.zeros((nw, NR, NB - 1), np.uint64)
+        _ck(lib().ea_sp_get_tempering(self.h, P(E), P(perm), P(acc), P(M)))
+        return E, perm, acc, M
+
+    def run(self, ncycles, ptfr=1, mesfr=1):
+        """ncycles x (ptfr sweeps + tempering); returns the energy averages
+        [nwords, 64, NR, NB] over the measurements."""
+        avg = np.zeros((self.g.nwords, 64, self.g.nrep, self.g.nbetas))
+        m = C.c_int32()
+        _ck(lib().ea_sp_run(self.h, ncycles, ptfr, mesfr, P(avg), C.byref(m)))
+        return avg / max(1, m.value)
+
+    def run_async(self, ncycles, ptfr=1, mesfr=1):
+        _ck(lib().ea_sp_run(self.h, ncycles, ptfr, mesfr, None, None))
+
+    def exact(self, betas=None):
+        """Density of states [nwords*64, 6V+1] and <E>(beta) [nwords*64, NB] (V <= 32)."""
+        b = np.ascontiguousarray(self.betas if betas is None else betas, np.float64)
+        ns = self.g.nwords * 64
+        dos = np.zeros((ns, 6 * self.V + 1), np.uint64)
+        mean = np.zeros((ns, len(b)))
+        _ck(lib().ea_sp_exact(self.h, P(b), len(b), P(dos), P(mean)))
+        return dos, mean

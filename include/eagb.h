@@ -334,6 +334,73 @@ int ea_server_drain(ea_server *s);
 /* Cancels queued jobs, waits for the running ones' bins and frees everything. */
 int ea_server_destroy(ea_server *s);
 
+/* ---- sample-packed layout: any L >= 2, Lz >= 2, any number of replicas -------
+ * No reference counterpart: the reference's multispin words hold 64 spatial
+ * sub-blocks of one sample, so L and Lz must be multiples of 8
+ * (header.h:41-47).  Here a word holds the same site of 64 disorder samples
+ * (bit b = sample b), so a job of `nwords` words simulates 64*nwords samples
+ * of any L x L x Lz tube.  The dynamics are the reference's, per sample: the
+ * Philox + heat-bath-threshold random words shared by all samples
+ * (main.cu:994-1150), the bit-sliced Metropolis rule (main.cu:1474-1506), six
+ * bond slots per site with the reference's fake bond on open z planes
+ * (ini.c:551-641; for odd L, see ea_sp_graph), E = 3V - 2 x unsatisfied bonds,
+ * and the tempering rule of upd.c:3-48 per (sample, replica) chain with a
+ * counter-based uniform.  Sites are updated colour by colour (a proper
+ * colouring of the bond graph: 2 colours when the tube is bipartite, else
+ * 3 or more).  Temperature slots keep their beta; accepted swaps move the
+ * samples' configurations between slots.
+ *
+ * Layouts: spins [nwords][V][NR][NB] (slot-major last), couplings
+ * [nwords][V][6] (slots +x,+y,+z,-x,-y,-z; both ends of a bond hold the same
+ * word), energies and permutations [nwords][64][NR][NB], site = x + L*(y + L*z). */
+typedef struct {
+  int32_t L, Lz, nbetas, nrep, nwords, bc;  /* bc: EA_PBC or EA_OBC; nbetas <= 64 */
+} ea_sp_geom;
+typedef struct ea_sp ea_sp;
+
+/* Bond graph (host only): nb [V][6] neighbour of each slot, mate [V][6] the
+ * half-edge p*6+slot at the other end, colour [V], ncol.  Any pointer may be
+ * NULL.  Open z planes: the missing z slot holds a fake bond; for even L to
+ * the y neighbour chosen by the parity of x+y+z (as the reference pairs
+ * them); for odd L to x+-1 (x < L-1), else y+-1 (y < L-1), and site
+ * (L-1, L-1) pairs with the same site of the other open plane. */
+int ea_sp_graph(int32_t L, int32_t Lz, int32_t bc, int32_t *nb, int32_t *mate, uint8_t *colour, int32_t *ncol);
+/* Couplings and initial spins as ea_sp_init makes them (host only). */
+int ea_sp_host_init(const ea_sp_geom *g, uint64_t seed_J, uint64_t seed_u, uint64_t *J, uint64_t *S);
+int ea_sp_create(const ea_sp_geom *g, int32_t device, ea_sp **out);
+int ea_sp_destroy(ea_sp *job);
+int ea_sp_info(const ea_sp *job, int32_t *ncol, int32_t *tile);
+int ea_sp_stream(ea_sp *job, void **stream);
+int ea_sp_sync(ea_sp *job);
+int ea_sp_set_temperatures(ea_sp *job, const double *betas, const uint64_t *cum);
+/* seeds: seed_J, seed_u, seed_MC (Metropolis generators per replica, as
+ * Init_Random seeds them), seed_PT (tempering uniforms). */
+int ea_sp_init(ea_sp *job, const uint64_t seeds[4], uint32_t jobid);
+int ea_sp_set_generators(ea_sp *job, const ea_generators *gen, uint64_t pt_seed);
+int ea_sp_get_generators(ea_sp *job, ea_generators *gen);
+int ea_sp_set_spins(ea_sp *job, const uint64_t *S);
+int ea_sp_get_spins(ea_sp *job, uint64_t *S);
+int ea_sp_set_couplings(ea_sp *job, const uint64_t *J);
+/* Colour-pass counter (Philox time) and tempering step counter. */
+int ea_sp_set_counter(ea_sp *job, int64_t iter, uint64_t ptstep, uint32_t jobid);
+int ea_sp_get_counter(ea_sp *job, int64_t *iter, uint64_t *ptstep);
+/* n Metropolis sweeps (every colour pass). */
+int ea_sp_sweeps(ea_sp *job, int32_t n);
+/* Unsatisfied half-edges U2 [nwords][64][NR][NB] (E = 3V - U2); NULL: on the device only. */
+int ea_sp_energy(ea_sp *job, int32_t *U2);
+/* Energies, then one tempering step for every chain, then the swaps applied to the spins. */
+int ea_sp_parallel_tempering(ea_sp *job);
+/* E and perm [nwords][64][NR][NB] after the last step, accepted swaps
+ * [nwords][64][NR][NB-1], lane masks of the last step [nwords][NR][NB-1]. */
+int ea_sp_get_tempering(ea_sp *job, int32_t *E, uint8_t *perm, uint32_t *acc, uint64_t *masks);
+/* ncycles x (ptfr sweeps + tempering); every mesfr cycles the energies of
+ * the slots are added to avgE [nwords][64][NR][NB] (sums; nmeas = count). */
+int ea_sp_run(ea_sp *job, int32_t ncycles, int32_t ptfr, int32_t mesfr, double *avgE, int32_t *nmeas);
+/* Exact enumeration (V <= 32): dos [nwords*64][6V+1] configurations with
+ * spin 0 up at each E = -3V..3V, and meanE [nwords*64][nbeta] = <E>(beta)
+ * from it in FP64 on the GPU. */
+int ea_sp_exact(ea_sp *job, const double *betas, int32_t nbeta, uint64_t *dos, double *meanE);
+
 /* cuRAND XORWOW uniforms (device generator) for a seed/offset, copied to host.
  * Used to check the device generator against the host one. */
 int ea_curand_uniforms(int32_t device, uint64_t seed, uint64_t offset, uint64_t n, double *out);

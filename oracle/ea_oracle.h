@@ -159,6 +159,16 @@ void or_state_release(or_state *st);
 int or_run_bin(or_state *st, const or_run_cfg *cfg, uint64_t *iter);
 int or_curand_host(uint64_t seed, uint64_t offset, uint64_t n, double *out);
 
+/* Sample-packed layout (sp_oracle.c): 64 samples per word, any L, Lz. */
+void or_sp_pass(int V, int NR, int NB, int nw, const int32_t *nb, const int32_t *sites, int nsites,
+                const uint32_t *ctr, const uint32_t *keys, const uint64_t *cum, const uint64_t *J, uint64_t *S);
+void or_sp_energy(int V, int NR, int NB, int nw, const int32_t *nb, const uint64_t *J, const uint64_t *S,
+                  int32_t *U2);
+void or_sp_pt(int V, int NR, int NB, int nw, const double *betas, const double *exptab, const int32_t *expoff,
+              uint64_t step, uint64_t seed, const int32_t *U2, int32_t *E, uint8_t *perm, uint32_t *acc,
+              uint64_t *masks, uint64_t *S);
+void or_sp_dos(int V, const int32_t *nb, const uint64_t *J, int w, int lane, uint64_t *hist);
+
 #ifdef __cplusplus
 }
 #endif

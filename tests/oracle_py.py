@@ -4,6 +4,7 @@ Test infrastructure: only tests/, __graft_entry__.smoke() and bench.py's
 reference leg use this module.  It builds the oracle on first use.
 """
 import ctypes as C
+import math
 import os
 import subprocess
 
@@ -60,8 +61,8 @@ _lib = None
 def lib():
     global _lib
     if _lib is None:
-        src = os.path.join(ORACLE_DIR, "ea_oracle.c")
-        if (not os.path.exists(LIB_PATH)) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+        srcs = [os.path.join(ORACLE_DIR, f) for f in ("ea_oracle.c", "sp_oracle.c", "ea_oracle.h")]
+        if (not os.path.exists(LIB_PATH)) or os.path.getmtime(LIB_PATH) < max(os.path.getmtime(f) for f in srcs):
             subprocess.run(["make", "-s", "-C", ORACLE_DIR, "libea_oracle.so"], check=True)
         _lib = C.CDLL(LIB_PATH)
         _lib.or_hq_next.restype = C.c_uint64
@@ -262,3 +263,51 @@ def curand_host(seed, offset, n):
     if lib().or_curand_host(C.c_uint64(seed), C.c_uint64(offset), C.c_uint64(n), ptr(out)) != 0:
         raise RuntimeError("cuRAND host generator failed")
     return out
+
+
+# ---------------------------------------------------------------------------
+# Sample-packed layout (oracle/sp_oracle.c)
+# ---------------------------------------------------------------------------
+def sp_exp_table(betas):
+    """exp(pt) of every tempering exponent that can change a decision, with
+    the host libm, per beta pair (offsets) -- dE = -2, -4, ... down to pt = -50."""
+    vals, off = [], []
+    for i in range(len(betas) - 1):
+        off.append(len(vals))
+        j = 1
+        while True:
+            dE = float(-2 * j)
+            pt = -(float(betas[i + 1]) - float(betas[i])) * dE
+            if not pt < 0 or pt < -50.0 or j > (1 << 22):
+                break
+            vals.append(math.exp(pt))
+            j += 1
+    off.append(len(vals))
+    return np.array(vals, np.float64), np.array(off, np.int32)
+
+
+def sp_pass(V, NR, NB, nw, nb, sites, ctr, keys, cum, J, S):
+    lib().or_sp_pass(V, NR, NB, nw, ptr(nb), ptr(sites), len(sites), ptr(ctr), ptr(keys), ptr(cum), ptr(J), ptr(S))
+
+
+def sp_energy(V, NR, NB, nw, nb, J, S):
+    U2 = np.zeros((nw, 64, NR, NB), np.int32)
+    lib().or_sp_energy(V, NR, NB, nw, ptr(nb), ptr(J), ptr(S), ptr(U2))
+    return U2
+
+
+def sp_pt(V, NR, NB, nw, betas, step, seed, U2, perm, acc, S):
+    """One tempering step (in place on perm, acc and S); returns E, masks."""
+    tab, off = sp_exp_table(betas)
+    E = np.zeros((nw, 64, NR, NB), np.int32)
+    masks = np.zeros((nw, NR, NB - 1), np.uint64)
+    b = np.ascontiguousarray(betas, np.float64)
+    lib().or_sp_pt(V, NR, NB, nw, ptr(b), ptr(tab), ptr(off), C.c_uint64(step), C.c_uint64(seed), ptr(U2), ptr(E),
+                   ptr(perm), ptr(acc), ptr(masks), ptr(S))
+    return E, masks
+
+
+def sp_dos(V, nb, J, w, lane):
+    h = np.zeros(6 * V + 1, np.uint64)
+    lib().or_sp_dos(V, ptr(nb), ptr(J), w, lane, ptr(h))
+    return h

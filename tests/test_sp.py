@@ -1,0 +1,256 @@
+"""Sample-packed layout (ea_sp_*): 64 disorder samples per word, tubes of any
+L >= 2 and Lz >= 2.
+
+CPU: the bond graph (slots, fake bonds of the open planes, mates, colouring),
+the couplings' symmetry, and the oracle's density of states against a plain
+enumeration.  GPU: colour passes, energies, tempering steps and whole runs
+bit for bit against the oracle (oracle/sp_oracle.c); the density of states
+against the oracle; and the Monte Carlo <E>(T) at 3x3x3 against exact
+enumeration of all 2^27 configurations, within its statistical error."""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+import oracle_py as O
+from conftest import ROOT
+
+import importlib.util
+
+spec = importlib.util.spec_from_file_location("eagb", os.path.join(ROOT, "ea-lcd-mc_gb300", "eagb.py"))
+eagb = importlib.util.module_from_spec(spec)
+spec.loader.exec_module(eagb)
+
+GOLD = os.path.join(ROOT, "tests", "golden")
+SEEDS = (0x1234567890ABCDEF, 0x0FEDCBA987654321, 0x1111222233334444, 0x5555666677778888)
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    import subprocess
+    import sys
+    subprocess.run([sys.executable, os.path.join(ROOT, "ea-lcd-mc_gb300", "build.py")], check=True,
+                   stdout=subprocess.DEVNULL)
+
+
+def lut(name):
+    d = np.load(os.path.join(GOLD, "lut_%s.npz" % name))
+    return d["betas"], d["cum"]
+
+
+GEOMS = [(2, 2, eagb.EA_PBC), (3, 3, eagb.EA_PBC), (3, 3, eagb.EA_OBC), (4, 5, eagb.EA_PBC), (5, 7, eagb.EA_OBC),
+         (6, 24, eagb.EA_PBC), (12, 48, eagb.EA_OBC), (7, 4, eagb.EA_OBC), (9, 2, eagb.EA_OBC), (2, 3, eagb.EA_OBC),
+         (8, 16, eagb.EA_OBC)]
+
+
+@pytest.mark.parametrize("L,Lz,bc", GEOMS)
+def test_graph(L, Lz, bc):
+    nb, mate, col, ncol = eagb.sp_graph(L, Lz, bc)
+    V = L * L * Lz
+    h = np.arange(6 * V)
+    m = mate.reshape(-1)
+    assert np.array_equal(m[m], h)                      # mates form an involution
+    assert np.array_equal(nb.reshape(-1)[m], h // 6)    # the mate sits at the neighbour
+    assert np.all(col[nb] != col[:, None])             # proper colouring (no self bonds)
+    bip = L % 2 == 0 and (bc == eagb.EA_OBC or Lz % 2 == 0)
+    assert ncol == (2 if bip else 3)
+    x, y, z = np.arange(V) % L, (np.arange(V) // L) % L, np.arange(V) // (L * L)
+    site = lambda xx, yy, zz: xx % L + L * (yy % L + L * (zz % Lz))
+    assert np.array_equal(nb[:, 0], site(x + 1, y, z)) and np.array_equal(nb[:, 3], site(x - 1, y, z))
+    assert np.array_equal(nb[:, 1], site(x, y + 1, z)) and np.array_equal(nb[:, 4], site(x, y - 1, z))
+    inner_up = (bc == eagb.EA_PBC) | (z < Lz - 1)
+    inner_dn = (bc == eagb.EA_PBC) | (z > 0)
+    assert np.array_equal(nb[inner_up, 2], site(x, y, z + 1)[inner_up])
+    assert np.array_equal(nb[inner_dn, 5], site(x, y, z - 1)[inner_dn])
+    if bc == eagb.EA_OBC:
+        top, bot = z == Lz - 1, z == 0
+        if L % 2 == 0:
+            # the reference's pairing: +y for even x+y+z, -y for odd
+            even = (x + y + z) % 2 == 0
+            want = np.where(even, site(x, y + 1, z), site(x, y - 1, z))
+            assert np.array_equal(nb[top, 2], want[top]) and np.array_equal(nb[bot, 5], want[bot])
+        else:
+            corner = (x == L - 1) & (y == L - 1)
+            assert np.array_equal(nb[top & corner, 2], site(x, y, 0)[top & corner])
+            assert np.array_equal(nb[bot & corner, 5], site(x, y, Lz - 1)[bot & corner])
+
+
+def test_couplings_and_spins():
+    g = eagb.SpGeom(5, 7, 4, 3, 2, eagb.EA_OBC)
+    nb, mate, col, ncol = eagb.sp_graph(5, 7, eagb.EA_OBC)
+    J, S = eagb.sp_host_init(g, 11, 22)
+    Jf = J.reshape(2, -1)
+    assert np.array_equal(Jf[:, mate.reshape(-1)], Jf)  # both ends of a bond hold the same word
+    assert J.shape == (2, 5 * 5 * 7, 6) and S.shape == (2, 5 * 5 * 7, 3, 4)
+    # couplings are +-J with p = 1/2 per bit
+    bits = np.unpackbits(Jf.view(np.uint8)).mean()
+    assert abs(bits - 0.5) < 0.01
+    J2, S2 = eagb.sp_host_init(g, 11, 22)
+    assert np.array_equal(J, J2) and np.array_equal(S, S2)
+
+
+def brute_dos(nb, J, lane):
+    """Plain enumeration from the definition: E = 3V - (unsatisfied half-edges)."""
+    V = nb.shape[0]
+    c = np.arange(1 << (V - 1), dtype=np.int64) << 1
+    spins = (c[:, None] >> np.arange(V)) & 1
+    jb = ((J[0] >> np.uint64(lane)) & np.uint64(1)).astype(np.int64)
+    U2 = np.zeros(len(c), np.int64)
+    for d in range(6):
+        U2 += (spins ^ spins[:, nb[:, d]] ^ jb[:, d][None, :]).sum(1)
+    return np.bincount(6 * V - U2, minlength=6 * V + 1).astype(np.uint64)
+
+
+@pytest.mark.parametrize("L,Lz,bc", [(2, 2, eagb.EA_PBC), (2, 3, eagb.EA_OBC), (2, 4, eagb.EA_PBC)])
+def test_oracle_dos_small(L, Lz, bc):
+    nb, mate, col, ncol = eagb.sp_graph(L, Lz, bc)
+    g = eagb.SpGeom(L, Lz, 2, 1, 1, bc)
+    J, _ = eagb.sp_host_init(g, 5, 6)
+    V = L * L * Lz
+    for lane in (0, 17, 63):
+        h = O.sp_dos(V, nb, J, 0, lane)
+        assert np.array_equal(h, brute_dos(nb, J, lane))
+        assert h.sum() == 1 << (V - 1)
+
+
+# ---------------------------------------------------------------------------
+# GPU
+# ---------------------------------------------------------------------------
+def oracle_gens(gen, NR):
+    prc = (O.HQ * NR).from_buffer_copy(bytes(memoryview(gen.prc).cast("B"))[:C.sizeof(O.HQ) * NR])
+    xo = (O.XO * NR).from_buffer_copy(bytes(memoryview(gen.xo).cast("B"))[:C.sizeof(O.XO) * NR])
+    keys = np.array(list(gen.keys)[:NR], np.uint32)
+    return prc, xo, keys
+
+
+class OracleSP:
+    """The oracle's copy of a job: passes, energies, tempering."""
+
+    def __init__(self, job, jobid):
+        g = job.g
+        self.L, self.Lz, self.NR, self.NB, self.nw = g.L, g.Lz, g.nrep, g.nbetas, g.nwords
+        self.V = job.V
+        self.nb, _, self.col, self.ncol = eagb.sp_graph(g.L, g.Lz, g.bc)
+        self.J, S0 = eagb.sp_host_init(g, SEEDS[0], SEEDS[1])
+        self.S = job.get_spins()
+        assert np.array_equal(self.S, S0)
+        self.prc, self.xo, self.keys = oracle_gens(job.get_generators(), self.NR)
+        self.betas, self.cum = job.betas, job.cum
+        self.sites = [np.nonzero(self.col == c)[0].astype(np.int32) for c in range(self.ncol)]
+        self.it, self.step, self.jobid = 0, 0, jobid
+        self.perm = np.tile(np.arange(self.NB, dtype=np.uint8), (self.nw, 64, self.NR, 1))
+        self.acc = np.zeros((self.nw, 64, self.NR, self.NB - 1), np.uint32)
+
+    def sweeps(self, n):
+        for _ in range(n):
+            for c in range(self.ncol):
+                ctr = O.fill_bits(self.prc, self.xo, self.NR, self.it, self.jobid)
+                O.sp_pass(self.V, self.NR, self.NB, self.nw, self.nb, self.sites[c], ctr, self.keys, self.cum,
+                          self.J, self.S)
+                self.it += 1
+
+    def energy(self):
+        return O.sp_energy(self.V, self.NR, self.NB, self.nw, self.nb, self.J, self.S)
+
+    def pt(self):
+        U2 = self.energy()
+        E, M = O.sp_pt(self.V, self.NR, self.NB, self.nw, self.betas, self.step, SEEDS[3], U2, self.perm,
+                       self.acc, self.S)
+        self.step += 1
+        return E, M
+
+
+def new_job(L, Lz, bc, lutname, NR, nw, jobid=3):
+    betas, cum = lut(lutname)
+    job = eagb.SpJob(L, Lz, betas, cum, nrep=NR, nwords=nw, bc=bc, seeds=SEEDS, jobid=jobid)
+    job.cum = np.ascontiguousarray(cum, np.uint64)
+    return job
+
+
+CASES = [(6, 8, eagb.EA_PBC, "T08_16_N4", 2, 2), (5, 7, eagb.EA_OBC, "T07_16_N6", 3, 1),
+         (3, 3, eagb.EA_PBC, "T07_16_N8", 2, 1), (12, 16, eagb.EA_OBC, "T07_16_N12", 4, 1),
+         (8, 16, eagb.EA_OBC, "T07_16_N24", 2, 3)]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("L,Lz,bc,ln,NR,nw", CASES)
+def test_sweeps_energy_tempering_match_oracle(L, Lz, bc, ln, NR, nw):
+    job = new_job(L, Lz, bc, ln, NR, nw)
+    orc = OracleSP(job, 3)
+    job.sweeps(2)
+    orc.sweeps(2)
+    assert np.array_equal(job.get_spins(), orc.S)
+    assert np.array_equal(job.energy(), orc.energy())
+    for _ in range(2):
+        job.parallel_tempering()
+        E, M = orc.pt()
+        gE, gperm, gacc, gM = job.tempering()
+        assert np.array_equal(gE, E)
+        assert np.array_equal(gM, M)
+        assert np.array_equal(gperm, orc.perm)
+        assert np.array_equal(gacc, orc.acc)
+        assert np.array_equal(job.get_spins(), orc.S)
+        job.sweeps(1)
+        orc.sweeps(1)
+    assert job.counter() == (orc.it, orc.step)
+    # the swaps did move configurations: some lane changed slot
+    assert orc.acc.sum() > 0
+    job.close()
+
+
+@pytest.mark.gpu
+def test_run_matches_oracle():
+    job = new_job(5, 6, eagb.EA_PBC, "T07_16_N6", 2, 2)
+    orc = OracleSP(job, 3)
+    avg = job.run(4, ptfr=2, mesfr=2)
+    tot = np.zeros((2, 64, 2, 6))
+    for cy in range(4):
+        orc.sweeps(2)
+        E, _ = orc.pt()
+        if (cy + 1) % 2 == 0:
+            tot += E
+    assert np.array_equal(job.get_spins(), orc.S)
+    assert np.array_equal(avg, tot / 2)
+    job.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("bc", [eagb.EA_PBC, eagb.EA_OBC])
+def test_exact_dos_matches_oracle(bc):
+    job = new_job(3, 3, bc, "T07_16_N8", 2, 1)
+    dos, mean = job.exact()
+    V = 27
+    assert np.all(dos.sum(1) == 1 << (V - 1))
+    nb, _, _, _ = eagb.sp_graph(3, 3, bc)
+    J, _ = eagb.sp_host_init(job.g, SEEDS[0], SEEDS[1])
+    for lane in (0, 41):
+        assert np.array_equal(dos[lane], O.sp_dos(V, nb, J, 0, lane))
+    # <E>(beta) from the histogram, recomputed on the host
+    E = np.arange(-3 * V, 3 * V + 1)
+    for lane in (0, 41):
+        g = dos[lane].astype(np.float64)
+        for k, b in enumerate(job.betas):
+            w = g * np.exp(b * (E - E[g > 0].max()))
+            assert abs((w * E).sum() / w.sum() - mean[lane, k]) < 1e-9 * V
+    job.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("bc", [eagb.EA_PBC, eagb.EA_OBC])
+def test_monte_carlo_matches_exact_enumeration(bc):
+    """3x3x3, 64 samples, 8 temperatures in [0.7, 1.6], 2 replicas, tempering
+    every sweep: the time average of E per sample and temperature agrees with
+    exact enumeration within the statistical error of 40 blocks."""
+    job = new_job(3, 3, bc, "T07_16_N8", 2, 1)
+    _, exact = job.exact()
+    job.run(4000)   # equilibration
+    nblk = 20
+    blocks = np.stack([job.run(1500) for _ in range(nblk)])         # [blk, 1, 64, NR, NB]
+    est = blocks[:, 0].transpose(0, 2, 1, 3).reshape(nblk * 2, 64, -1)  # blocks x replicas
+    mean = est.mean(0)
+    err = est.std(0, ddof=1) / np.sqrt(est.shape[0])
+    z = (mean - exact) / np.maximum(err, 1e-12)
+    assert np.abs(z).max() < 6.0, np.abs(z).max()
+    assert 0.5 < (z ** 2).mean() < 2.0, (z ** 2).mean()
+    job.close()
