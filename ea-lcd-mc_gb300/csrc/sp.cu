@@ -245,6 +245,120 @@ __global__ void k_sp_measure(const __grid_constant__ SpDev d) {
 }
 
 // ---------------------------------------------------------------------------
+// Houdayer move (main.cu:351-453, HoudayerXEA.cu:54-374), per sample.
+// Replica pairs: as the reference picks them (main.cu:408-421) from random_c,
+// in two groups of NR/2 replicas (one group of NR when NR < 4).  For each
+// group and each slot b < nclust, the overlap q = s_r1 ^ s_r2 of every sample
+// is split into maximal clusters of equal q along all six bond slots (the
+// fake bonds of open planes included, so every move conserves E(r1)+E(r2)
+// for any L; for even L the fake bonds duplicate y bonds and the clusters
+// are the reference's); a cluster's root is its smallest site index, as in
+// the reference, and each cluster flips in both replicas with probability
+// 1/2.  The coin of a cluster is the lowest bit of Philox4x32-10 of (move,
+// root, sample, slot, group) -- the reference compares a cuRAND uniform per
+// (sample, beta, root) with 0.5 (HoudayerXEA.cu:373); a counter-based bit
+// needs no V*NB uniforms per sample.
+// ---------------------------------------------------------------------------
+__global__ void k_sp_pairs(const __grid_constant__ SpDev d) {
+  if (threadIdx.x) return;
+  *d.move += 1ull;
+  const int ng = d.NR >= 4 ? 2 : 1, h = d.NR / ng;
+  for (int g = 0; g < ng; ++g) {
+    int idx[64];
+    for (int k = 0; k < h; ++k) idx[k] = k + g * h;
+    for (int k = 0; k < h - 1; ++k) {
+      const u64 f = d_hq_next(d.rc);
+      const int q = k + (int)(((uint32_t)(f >> 32)) % (uint32_t)(h - k));
+      const int t = idx[k]; idx[k] = idx[q]; idx[q] = t;
+    }
+    d.pairs[2 * g] = idx[0];
+    d.pairs[2 * g + 1] = idx[1];
+  }
+}
+
+__global__ void k_sp_overlap(const __grid_constant__ SpDev d, int g) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // (w, b, site)
+  const int V = d.V, nc = d.nclust;
+  if (t >= (long long)d.nw * nc * V) return;
+  const int i = (int)(t % V), b = (int)((t / V) % nc), w = (int)(t / ((long long)V * nc));
+  const int r1 = d.pairs[2 * g], r2 = d.pairs[2 * g + 1];
+  const u64 *p = d.S + (((size_t)w * V + i) * d.NR) * d.NB + b;
+  d.Q[t] = p[(size_t)r1 * d.NB] ^ p[(size_t)r2 * d.NB];
+}
+
+__device__ __forceinline__ uint32_t sp_find(const uint32_t *lab, uint32_t x) {
+  uint32_t y = lab[x];
+  while (y != x) { x = y; y = lab[x]; }
+  return x;
+}
+
+// One CTA per (word, slot, sample) lattice: labels in SMEM, atomicMin hooking
+// of roots (a root only ever points to a smaller index, so each cluster ends
+// at its smallest site) until a round joins nothing, then the flips.
+__global__ void __launch_bounds__(1024) k_sp_cluster(const __grid_constant__ SpDev d, int g, unsigned long long key) {
+  extern __shared__ uint32_t sm[];
+  const int V = d.V, nc = d.nclust, nq = (V + 31) / 32;
+  uint32_t *lab = sm, *qb = sm + V, *sel = qb + nq;
+  const int lane = blockIdx.x & 63, lat = blockIdx.x >> 6;  // lat = w * nc + b
+  const int b = lat % nc, w = lat / nc;
+  const u64 *Q = d.Q + (size_t)lat * V;
+  for (int i0 = threadIdx.x & ~31; i0 < nq * 32; i0 += blockDim.x) {
+    const int i = i0 + (threadIdx.x & 31);
+    const unsigned bit = i < V ? (unsigned)((Q[i] >> lane) & 1ull) : 0u;
+    const unsigned m = __ballot_sync(0xffffffffu, bit);
+    if ((threadIdx.x & 31) == 0) qb[i0 >> 5] = m;
+  }
+  for (int i = threadIdx.x; i < V; i += blockDim.x) lab[i] = (uint32_t)i;
+  for (int i = threadIdx.x; i < nq; i += blockDim.x) sel[i] = 0;
+  __syncthreads();
+  for (;;) {
+    int changed = 0;
+    for (int i = threadIdx.x; i < V; i += blockDim.x) {
+      const unsigned qi = (qb[i >> 5] >> (i & 31)) & 1u;
+#pragma unroll
+      for (int q = 0; q < 6; ++q) {
+        const int p = __ldg(d.nb + (size_t)i * 6 + q);
+        if (p < i && ((qb[p >> 5] >> (p & 31)) & 1u) == qi) {
+          const uint32_t a = sp_find(lab, (uint32_t)i), c = sp_find(lab, (uint32_t)p);
+          if (a != c) {
+            atomicMin(&lab[max(a, c)], min(a, c));
+            changed = 1;
+          }
+        }
+      }
+    }
+    if (!__syncthreads_or(changed)) break;
+  }
+  for (int i = threadIdx.x; i < V; i += blockDim.x) lab[i] = sp_find(lab, (uint32_t)i);
+  __syncthreads();
+  const unsigned long long mv = *d.move;
+  const uint32_t tag = (((uint32_t)(w * 64 + lane) << 6 | (uint32_t)b) << 1) | (uint32_t)g;
+  for (int i = threadIdx.x; i < V; i += blockDim.x) {
+    if (lab[i] != (uint32_t)i) continue;
+    uint32_t v0 = (uint32_t)mv, v1 = (uint32_t)(mv >> 32), v2 = (uint32_t)i, v3 = tag;
+    philox10(v0, v1, v2, v3, (uint32_t)key, (uint32_t)(key >> 32));
+    if (v0 & 1u) atomicOr(&sel[i >> 5], 1u << (i & 31));
+  }
+  __syncthreads();
+  const int r1 = d.pairs[2 * g], r2 = d.pairs[2 * g + 1];
+  const u64 bitw = 1ull << lane;
+  for (int i = threadIdx.x; i < V; i += blockDim.x) {
+    const uint32_t r = lab[i];
+    if ((sel[r >> 5] >> (r & 31)) & 1u) {
+      u64 *p = d.S + (((size_t)w * V + i) * d.NR) * d.NB + b;
+      atomicXor(p + (size_t)r1 * d.NB, bitw);
+      atomicXor(p + (size_t)r2 * d.NB, bitw);
+    }
+  }
+}
+
+// Energy measurement of a bin's iteration: avgE += 3V - U2 (slot order).
+__global__ void k_sp_measure_u2(const __grid_constant__ SpDev d) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < (long long)d.nw * 64 * d.NR * d.NB) d.avgE[i] += (double)(3 * d.V - d.U2[i]);
+}
+
+// ---------------------------------------------------------------------------
 // Exact enumeration: for every sample of every word, the number of spin
 // configurations at each energy E = 3V - U2 among the 2^(V-1) with spin 0 up
 // (E is even under the global flip, so the full counts are twice these; the
@@ -322,6 +436,8 @@ __global__ void k_sp_exact(const __grid_constant__ SpDev d, const double *betas,
 // ---------------------------------------------------------------------------
 // Launchers
 // ---------------------------------------------------------------------------
+size_t sp_cluster_smem(int V);
+
 size_t sp_sweep_smem(int NB, int NR, int kt) {
   return (size_t)NB * 256 * 10 + (size_t)3 * NB * kt * NR * 8 + (size_t)kt * 7 * 4;
 }
@@ -339,7 +455,11 @@ int sp_kt(int NB, int NR, int nsites_colour) {
 }
 
 cudaError_t sp_setup() {
-  return cudaFuncSetAttribute(k_sp_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  cudaError_t e = cudaFuncSetAttribute(k_sp_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_sp_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sp_cluster_smem(kSpClusterMaxV));
+  return e;
 }
 
 cudaError_t sp_launch_pass(const SpDev &d, int colour, int off, int n, cudaStream_t st) {
@@ -375,6 +495,26 @@ cudaError_t sp_launch_permute(const SpDev &d, cudaStream_t st) {
 cudaError_t sp_launch_measure(const SpDev &d, cudaStream_t st) {
   const long long n = (long long)d.nw * 64 * d.NR * d.NB;
   k_sp_measure<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d);
+  return cudaGetLastError();
+}
+
+size_t sp_cluster_smem(int V) { return ((size_t)V + 2 * (size_t)((V + 31) / 32)) * 4; }
+
+cudaError_t sp_launch_houdayer(const SpDev &d, cudaStream_t st) {
+  k_sp_pairs<<<1, 32, 0, st>>>(d);
+  const int ng = d.NR >= 4 ? 2 : 1;
+  const unsigned long long key = d.pt_seed ^ 0xC2B2AE3585EBCA6BULL;
+  for (int g = 0; g < ng; ++g) {
+    const long long n = (long long)d.nw * d.nclust * d.V;
+    k_sp_overlap<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d, g);
+    k_sp_cluster<<<(unsigned)(d.nw * d.nclust * 64), 1024, sp_cluster_smem(d.V), st>>>(d, g, key);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t sp_launch_measure_u2(const SpDev &d, cudaStream_t st) {
+  const long long n = (long long)d.nw * 64 * d.NR * d.NB;
+  k_sp_measure_u2<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d);
   return cudaGetLastError();
 }
 
@@ -510,6 +650,9 @@ int ea_sp_create(const ea_sp_geom *gp, int32_t device, ea_sp **out) {
   { int32_t *p; SOWN(p, (size_t)d.NB); d.expoff = p; }
   SOWN(d.ptstep, 1);
   SOWN(d.avgE, nw * 64 * G);
+  SOWN(d.rc, 1);
+  SOWN(d.pairs, 4);
+  SOWN(d.move, 1);
 #undef SOWN
   SCU(cudaMemcpyAsync((void *)d.nb, g.nb.data(), V * 6 * 4, cudaMemcpyHostToDevice, c->st));
   SCU(cudaMemcpyAsync((void *)d.col_sites, g.col_sites.data(), V * 4, cudaMemcpyHostToDevice, c->st));
@@ -529,6 +672,7 @@ int ea_sp_destroy(ea_sp *c) {
   for (void *p : c->owned) cudaFree(p);
   if (c->exptab) cudaFree(c->exptab);
   if (c->d.dos) cudaFree(c->d.dos);
+  if (c->d.Q) cudaFree(c->d.Q);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
   return EA_OK;
@@ -589,6 +733,7 @@ int ea_sp_set_generators(ea_sp *c, const ea_generators *gen, uint64_t pt_seed) {
   SCU(cudaMemcpyAsync(c->d.prc, gen->prc, sizeof(ea_hq) * NR, cudaMemcpyHostToDevice, c->st));
   SCU(cudaMemcpyAsync(c->d.xo, gen->xo, sizeof(ea_xoshiro) * NR, cudaMemcpyHostToDevice, c->st));
   SCU(cudaMemcpyAsync((void *)c->d.keys, gen->keys, sizeof(uint32_t) * NR, cudaMemcpyHostToDevice, c->st));
+  SCU(cudaMemcpyAsync(c->d.rc, &gen->rc, sizeof(ea_hq), cudaMemcpyHostToDevice, c->st));
   SCU(cudaStreamSynchronize(c->st));
   c->d.pt_seed = pt_seed;
   return EA_OK;
@@ -602,6 +747,7 @@ int ea_sp_get_generators(ea_sp *c, ea_generators *gen) {
   SCU(cudaMemcpyAsync(gen->prc, c->d.prc, sizeof(ea_hq) * NR, cudaMemcpyDeviceToHost, c->st));
   SCU(cudaMemcpyAsync(gen->xo, c->d.xo, sizeof(ea_xoshiro) * NR, cudaMemcpyDeviceToHost, c->st));
   SCU(cudaMemcpyAsync(gen->keys, c->d.keys, sizeof(uint32_t) * NR, cudaMemcpyDeviceToHost, c->st));
+  SCU(cudaMemcpyAsync(&gen->rc, c->d.rc, sizeof(ea_hq), cudaMemcpyDeviceToHost, c->st));
   SCU(cudaStreamSynchronize(c->st));
   return EA_OK;
 }
@@ -620,6 +766,9 @@ int ea_sp_init(ea_sp *c, const uint64_t seeds[4], uint32_t jobid) {
   std::vector<ea_generators> gen(1);
   std::memset(gen.data(), 0, sizeof(ea_generators));
   for (int r = 0; r < d.NR; ++r) init_generators(sMC[r], gen[0].prc[r], gen[0].xo[r], gen[0].keys[r]);
+  // replica-pair generator of the cluster moves, a Parisi-Rapuano stream
+  // seeded from seed_PT as Init_Rand_HQ_64bits seeds one
+  hq_seed(gen[0].rc, seeds[3]);
   int rc = ea_sp_set_couplings(c, J.data());
   if (!rc) rc = ea_sp_set_spins(c, S.data());
   if (!rc) rc = ea_sp_set_generators(c, gen.data(), seeds[3]);
@@ -728,27 +877,52 @@ int ea_sp_get_tempering(ea_sp *c, int32_t *E, uint8_t *perm, uint32_t *acc, uint
   return EA_OK;
 }
 
-int ea_sp_run(ea_sp *c, int32_t ncycles, int32_t ptfr, int32_t mesfr, double *avgE, int32_t *nmeas) {
-  if (!c || ncycles < 0 || ptfr < 1 || mesfr < 1) return spfail(EA_ERR_ARG, "bad cadence");
+static int sp_houdayer(ea_sp *c, int nclust) {
+  SpDev &d = c->d;
+  if (d.NR < 2) return spfail(EA_ERR_ARG, "the Houdayer move needs 2 replicas");
+  if (d.V > kSpClusterMaxV) return spfail(EA_ERR_ARG, "cluster moves need V <= %d sites (V = %d)", kSpClusterMaxV, d.V);
+  if (nclust <= 0) nclust = (int)std::lround(0.5 * d.NB);
+  if (nclust > d.NB) nclust = d.NB;
+  if (nclust > d.nclust) {
+    SCU(cudaStreamSynchronize(c->st));
+    if (d.Q) cudaFree(d.Q);
+    d.Q = nullptr;
+    SCU(cudaMalloc((void **)&d.Q, sizeof(unsigned long long) * (size_t)d.nw * nclust * d.V));
+  }
+  d.nclust = nclust;
+  SCU(sp_launch_houdayer(d, c->st));
+  return EA_OK;
+}
+
+int ea_sp_houdayer(ea_sp *c, int32_t nclust) {
+  if (!c) return spfail(EA_ERR_ARG, "null job");
+  SCU(cudaSetDevice(c->device));
+  return sp_houdayer(c, nclust);
+}
+
+int ea_sp_run(ea_sp *c, const ea_cadence *cad, double *avgE) {
+  if (!c || !cad || cad->itmax < 1 || cad->houfr < 1 || cad->mesfr < 1 || cad->ptfr < 1)
+    return spfail(EA_ERR_ARG, "bad cadence");
   if (!c->have_temps) return spfail(EA_ERR_STATE, "temperatures not set");
   SCU(cudaSetDevice(c->device));
   const SpDev &d = c->d;
   const size_t n = (size_t)d.nw * 64 * d.NR * d.NB;
   SCU(cudaMemsetAsync(d.avgE, 0, n * 8, c->st));
-  int m = 0;
-  for (int cy = 0; cy < ncycles; ++cy) {
-    int rc = sp_sweeps(c, ptfr);
-    if (!rc) rc = sp_pt(c);
-    if (rc) return rc;
-    if ((cy + 1) % mesfr == 0) {
-      SCU(sp_launch_measure(d, c->st));
-      ++m;
+  int rc;
+  for (int it = 0; it < cad->itmax; ++it) {
+    for (int im = 0; im < cad->mesfr; ++im) {
+      for (int ih = 0; ih < cad->houfr; ++ih)
+        if ((rc = sp_sweeps(c, cad->ptfr)) || (rc = sp_pt(c))) return rc;
+      if (cad->cluster && (rc = sp_houdayer(c, cad->nclust))) return rc;
     }
+    SCU(sp_launch_energy(c->d, c->st));
+    SCU(sp_launch_measure_u2(c->d, c->st));
   }
-  if (nmeas) *nmeas = m;
   if (avgE) {
-    SCU(cudaMemcpyAsync(avgE, d.avgE, n * 8, cudaMemcpyDeviceToHost, c->st));
+    std::vector<double> h(n);
+    SCU(cudaMemcpyAsync(h.data(), d.avgE, n * 8, cudaMemcpyDeviceToHost, c->st));
     SCU(cudaStreamSynchronize(c->st));
+    for (size_t i = 0; i < n; ++i) avgE[i] = h[i] / cad->itmax;
   }
   return EA_OK;
 }

@@ -61,9 +61,18 @@ struct SpDev {
   unsigned long long *ptstep;        // tempering steps so far
   unsigned long long pt_seed;
   double *avgE;                      // [nw][64][NR][NB]
+  // Houdayer move
+  ea_hq *rc;                         // replica-pair generator (random_c)
+  int32_t *pairs;                    // [2 groups][2]
+  unsigned long long *Q;             // [nw][nclust][V] overlap words s_r1 ^ s_r2
+  unsigned long long *move;          // cluster moves so far
+  int nclust;
   // exact enumeration
   unsigned long long *dos;           // [nw][64][6V+1] states per energy (E = -3V..3V)
 };
+
+// Largest lattice of the one-CTA cluster labelling (labels in SMEM).
+constexpr int kSpClusterMaxV = 32768;
 
 int sp_kt(int NB, int NR, int nsites_colour);
 size_t sp_sweep_smem(int NB, int NR, int kt);
@@ -73,6 +82,8 @@ cudaError_t sp_launch_energy(const SpDev &d, cudaStream_t st);
 cudaError_t sp_launch_pt(const SpDev &d, cudaStream_t st);
 cudaError_t sp_launch_permute(const SpDev &d, cudaStream_t st);
 cudaError_t sp_launch_measure(const SpDev &d, cudaStream_t st);
+cudaError_t sp_launch_houdayer(const SpDev &d, cudaStream_t st);
+cudaError_t sp_launch_measure_u2(const SpDev &d, cudaStream_t st);
 cudaError_t sp_launch_dos(const SpDev &d, cudaStream_t st);
 cudaError_t sp_launch_exact(const SpDev &d, const double *betas, int nbeta, double *meanE, cudaStream_t st);
 

@@ -525,16 +525,20 @@ class SpJob:
         _ck(lib().ea_sp_get_tempering(self.h, P(E), P(perm), P(acc), P(M)))
         return E, perm, acc, M
 
-    def run(self, ncycles, ptfr=1, mesfr=1):
-        """ncycles x (ptfr sweeps + tempering); returns the energy averages
-        [nwords, 64, NR, NB] over the measurements."""
-        avg = np.zeros((self.g.nwords, 64, self.g.nrep, self.g.nbetas))
-        m = C.c_int32()
-        _ck(lib().ea_sp_run(self.h, ncycles, ptfr, mesfr, P(avg), C.byref(m)))
-        return avg / max(1, m.value)
+    def houdayer(self, nclust=0):
+        _ck(lib().ea_sp_houdayer(self.h, nclust))
 
-    def run_async(self, ncycles, ptfr=1, mesfr=1):
-        _ck(lib().ea_sp_run(self.h, ncycles, ptfr, mesfr, None, None))
+    def run_bin(self, itmax, houfr=1, mesfr=1, ptfr=1, cluster=False, nclust=0):
+        """One bin of the cadence; returns the bin's average energy of every
+        (word, sample, replica, slot)."""
+        avg = np.zeros((self.g.nwords, 64, self.g.nrep, self.g.nbetas))
+        cad = Cadence(itmax, houfr, mesfr, ptfr, int(cluster), nclust)
+        _ck(lib().ea_sp_run(self.h, C.byref(cad), P(avg)))
+        return avg
+
+    def run_async(self, itmax, houfr=1, mesfr=1, ptfr=1, cluster=False, nclust=0):
+        cad = Cadence(itmax, houfr, mesfr, ptfr, int(cluster), nclust)
+        _ck(lib().ea_sp_run(self.h, C.byref(cad), None))
 
     def exact(self, betas=None):
         """Density of states [nwords*64, 6V+1] and <E>(beta) [nwords*64, NB] (V <= 32)."""

@@ -393,9 +393,19 @@ int ea_sp_parallel_tempering(ea_sp *job);
 /* E and perm [nwords][64][NR][NB] after the last step, accepted swaps
  * [nwords][64][NR][NB-1], lane masks of the last step [nwords][NR][NB-1]. */
 int ea_sp_get_tempering(ea_sp *job, int32_t *E, uint8_t *perm, uint32_t *acc, uint64_t *masks);
-/* ncycles x (ptfr sweeps + tempering); every mesfr cycles the energies of
- * the slots are added to avgE [nwords][64][NR][NB] (sums; nmeas = count). */
-int ea_sp_run(ea_sp *job, int32_t ncycles, int32_t ptfr, int32_t mesfr, double *avgE, int32_t *nmeas);
+/* Houdayer move (main.cu:351-453) per sample, on the nclust coldest slots
+ * (<= 0: lround(NB/2)): replica pairs from random_c as the reference picks
+ * them (two groups of NR/2, one group when NR < 4), maximal clusters of equal
+ * overlap along all six bond slots (fake bonds included: E(r1)+E(r2) is
+ * conserved for any L), smallest-site roots, each cluster flipped in both
+ * replicas with probability 1/2 (a Philox bit of move, root, sample, slot,
+ * group).  V <= 32768 sites. */
+int ea_sp_houdayer(ea_sp *job, int32_t nclust);
+/* One bin of the reference's cadence (main.cu:149-230): itmax x [mesfr x
+ * (houfr x (ptfr sweeps + tempering) + Houdayer if cad->cluster) + energy
+ * measurement]; avgE [nwords][64][NR][NB] (may be NULL) = the bin's average
+ * energy of each slot. */
+int ea_sp_run(ea_sp *job, const ea_cadence *cad, double *avgE);
 /* Exact enumeration (V <= 32): dos [nwords*64][6V+1] configurations with
  * spin 0 up at each E = -3V..3V, and meanE [nwords*64][nbeta] = <E>(beta)
  * from it in FP64 on the GPU. */

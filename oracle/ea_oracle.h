@@ -168,6 +168,8 @@ void or_sp_pt(int V, int NR, int NB, int nw, const double *betas, const double *
               uint64_t step, uint64_t seed, const int32_t *U2, int32_t *E, uint8_t *perm, uint32_t *acc,
               uint64_t *masks, uint64_t *S);
 void or_sp_dos(int V, const int32_t *nb, const uint64_t *J, int w, int lane, uint64_t *hist);
+void or_sp_cluster(int V, int NR, int NB, int nw, const int32_t *nb, int nclust, int g, int r1, int r2,
+                   uint64_t move, uint64_t key, uint64_t *S);
 
 #ifdef __cplusplus
 }

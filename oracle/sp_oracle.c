@@ -175,3 +175,59 @@ void or_sp_dos(int V, const int32_t *nb, const uint64_t *J, int w, int lane, uin
     free(loc);
   }
 }
+
+/* One group of a Houdayer move on the slots b < nclust of every sample:
+ * q = s_r1 ^ s_r2, maximal clusters of equal q along the six bond slots,
+ * each labelled by its smallest site (a depth-first walk started from the
+ * sites in ascending order), flipped in both replicas when the lowest bit of
+ * Philox4x32-10((move, root, tag), key) is 1, tag = ((w*64 + lane) << 6 | b) << 1 | g. */
+void or_sp_cluster(int V, int NR, int NB, int nw, const int32_t *nb, int nclust, int g, int r1, int r2,
+                   uint64_t move, uint64_t key, uint64_t *S) {
+  const size_t G = (size_t)NR * NB;
+#pragma omp parallel
+  {
+    int32_t *root = (int32_t *)malloc(sizeof(int32_t) * V);
+    int32_t *stack = (int32_t *)malloc(sizeof(int32_t) * V);
+    uint8_t *q = (uint8_t *)malloc(V);
+#pragma omp for schedule(dynamic) collapse(3)
+    for (int w = 0; w < nw; w++)
+      for (int b = 0; b < nclust; b++)
+        for (int lane = 0; lane < 64; lane++) {
+          uint64_t *Sw = S + (size_t)w * V * G;
+          for (int i = 0; i < V; i++) {
+            const uint64_t x = Sw[(size_t)i * G + (size_t)r1 * NB + b] ^ Sw[(size_t)i * G + (size_t)r2 * NB + b];
+            q[i] = (uint8_t)((x >> lane) & 1ULL);
+            root[i] = -1;
+          }
+          for (int i = 0; i < V; i++) {
+            if (root[i] >= 0) continue;
+            int top = 0;
+            stack[top++] = i;
+            root[i] = i;
+            while (top) {
+              const int k = stack[--top];
+              for (int d = 0; d < 6; d++) {
+                const int p = nb[k * 6 + d];
+                if (root[p] < 0 && q[p] == q[i]) { root[p] = i; stack[top++] = p; }
+              }
+            }
+          }
+          const uint32_t tag = (((uint32_t)(w * 64 + lane) << 6 | (uint32_t)b) << 1) | (uint32_t)g;
+          for (int i = 0; i < V; i++) {
+            const int r = root[i];
+            uint32_t v[4] = {(uint32_t)move, (uint32_t)(move >> 32), (uint32_t)r, tag};
+            philox_pt(v, (uint32_t)key, (uint32_t)(key >> 32));
+            if (v[0] & 1u) {
+              const uint64_t bit = 1ULL << lane;
+#pragma omp atomic
+              Sw[(size_t)i * G + (size_t)r1 * NB + b] ^= bit;
+#pragma omp atomic
+              Sw[(size_t)i * G + (size_t)r2 * NB + b] ^= bit;
+            }
+          }
+        }
+    free(root);
+    free(stack);
+    free(q);
+  }
+}

@@ -311,3 +311,7 @@ def sp_dos(V, nb, J, w, lane):
     h = np.zeros(6 * V + 1, np.uint64)
     lib().or_sp_dos(V, ptr(nb), ptr(J), w, lane, ptr(h))
     return h
+
+
+def sp_cluster(V, NR, NB, nw, nb, nclust, g, r1, r2, move, key, S):
+    lib().or_sp_cluster(V, NR, NB, nw, ptr(nb), nclust, g, r1, r2, C.c_uint64(move), C.c_uint64(key), ptr(S))

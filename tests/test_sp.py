@@ -139,6 +139,9 @@ class OracleSP:
         self.betas, self.cum = job.betas, job.cum
         self.sites = [np.nonzero(self.col == c)[0].astype(np.int32) for c in range(self.ncol)]
         self.it, self.step, self.jobid = 0, 0, jobid
+        gen = job.get_generators()
+        self.rc = O.HQ.from_buffer_copy(bytes(memoryview(gen.rc).cast("B")))
+        self.move = 0
         self.perm = np.tile(np.arange(self.NB, dtype=np.uint8), (self.nw, 64, self.NR, 1))
         self.acc = np.zeros((self.nw, 64, self.NR, self.NB - 1), np.uint32)
 
@@ -159,6 +162,23 @@ class OracleSP:
                        self.acc, self.S)
         self.step += 1
         return E, M
+
+    def houdayer(self, nclust=0):
+        """Replica pairs drawn from random_c as main.cu:408-421 draws them, then
+        the cluster flips of each group."""
+        if nclust <= 0:
+            nclust = int(np.floor(0.5 * self.NB + 0.5))
+        self.move += 1
+        ng = 2 if self.NR >= 4 else 1
+        h = self.NR // ng
+        for g in range(ng):
+            idx = list(range(g * h, g * h + h))
+            for k in range(h - 1):
+                f = O.lib().or_hq_next(C.byref(self.rc))
+                q = k + ((f >> 32) % (h - k))
+                idx[k], idx[q] = idx[q], idx[k]
+            O.sp_cluster(self.V, self.NR, self.NB, self.nw, self.nb, nclust, g, idx[0], idx[1], self.move,
+                         SEEDS[3] ^ 0xC2B2AE3585EBCA6B, self.S)
 
 
 def new_job(L, Lz, bc, lutname, NR, nw, jobid=3):
@@ -200,18 +220,46 @@ def test_sweeps_energy_tempering_match_oracle(L, Lz, bc, ln, NR, nw):
 
 
 @pytest.mark.gpu
-def test_run_matches_oracle():
-    job = new_job(5, 6, eagb.EA_PBC, "T07_16_N6", 2, 2)
+@pytest.mark.parametrize("L,Lz,bc,NR,nw", [(5, 6, eagb.EA_OBC, 4, 2), (3, 3, eagb.EA_PBC, 2, 1), (4, 8, eagb.EA_OBC, 8, 1)])
+def test_houdayer_matches_oracle(L, Lz, bc, NR, nw):
+    job = new_job(L, Lz, bc, "T07_16_N6", NR, nw)
     orc = OracleSP(job, 3)
-    avg = job.run(4, ptfr=2, mesfr=2)
-    tot = np.zeros((2, 64, 2, 6))
-    for cy in range(4):
-        orc.sweeps(2)
-        E, _ = orc.pt()
-        if (cy + 1) % 2 == 0:
-            tot += E
+    for _ in range(3):
+        job.sweeps(1)
+        orc.sweeps(1)
+        job.parallel_tempering()
+        orc.pt()
+        before = job.energy()
+        job.houdayer(3)
+        orc.houdayer(3)
+        assert np.array_equal(job.get_spins(), orc.S)
+        after = job.energy()
+        # each move conserves E(r1) + E(r2) of every sample and slot: the sum
+        # over replicas is unchanged
+        assert np.array_equal(before.sum(2), after.sum(2))
+    # clusters did flip
+    assert not np.array_equal(before, after)
+    job.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cluster", [False, True])
+def test_run_bin_matches_oracle(cluster):
+    job = new_job(5, 6, eagb.EA_PBC, "T07_16_N6", 4, 2)
+    orc = OracleSP(job, 3)
+    itmax, houfr, mesfr, ptfr = 3, 2, 2, 2
+    avg = job.run_bin(itmax, houfr, mesfr, ptfr, cluster=cluster, nclust=0)
+    tot = np.zeros((2, 64, 4, 6))
+    for it in range(itmax):
+        for im in range(mesfr):
+            for ih in range(houfr):
+                orc.sweeps(ptfr)
+                orc.pt()
+            if cluster:
+                orc.houdayer(0)
+        tot += 3 * orc.V - orc.energy()
     assert np.array_equal(job.get_spins(), orc.S)
-    assert np.array_equal(avg, tot / 2)
+    assert np.array_equal(avg, tot / itmax)
     job.close()
 
 
@@ -237,17 +285,21 @@ def test_exact_dos_matches_oracle(bc):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("bc", [eagb.EA_PBC, eagb.EA_OBC])
-def test_monte_carlo_matches_exact_enumeration(bc):
-    """3x3x3, 64 samples, 8 temperatures in [0.7, 1.6], 2 replicas, tempering
-    every sweep: the time average of E per sample and temperature agrees with
-    exact enumeration within the statistical error of 40 blocks."""
-    job = new_job(3, 3, bc, "T07_16_N8", 2, 1)
+@pytest.mark.parametrize("bc,cluster", [(eagb.EA_PBC, False), (eagb.EA_OBC, False), (eagb.EA_PBC, True),
+                                        (eagb.EA_OBC, True)])
+def test_monte_carlo_matches_exact_enumeration(bc, cluster):
+    """3x3x3, 64 samples, 8 temperatures in [0.7, 1.6], tempering every sweep
+    (2 replicas), or with a Houdayer move every 5 sweeps (4 replicas): the
+    time average of E per sample and temperature agrees with exact
+    enumeration within the statistical error of the blocks."""
+    job = new_job(3, 3, bc, "T07_16_N8", 4 if cluster else 2, 1)
+    NR = job.g.nrep
     _, exact = job.exact()
-    job.run(4000)   # equilibration
+    cad = dict(houfr=5, mesfr=1, ptfr=1, cluster=cluster)
+    job.run_bin(800, **cad)   # equilibration
     nblk = 20
-    blocks = np.stack([job.run(1500) for _ in range(nblk)])         # [blk, 1, 64, NR, NB]
-    est = blocks[:, 0].transpose(0, 2, 1, 3).reshape(nblk * 2, 64, -1)  # blocks x replicas
+    blocks = np.stack([job.run_bin(300, **cad) for _ in range(nblk)])     # [blk, 1, 64, NR, NB]
+    est = blocks[:, 0].transpose(0, 2, 1, 3).reshape(nblk * NR, 64, -1)  # blocks x replicas
     mean = est.mean(0)
     err = est.std(0, ddof=1) / np.sqrt(est.shape[0])
     z = (mean - exact) / np.maximum(err, 1e-12)
