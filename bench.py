@@ -309,6 +309,47 @@ def run_serve(args, dev, eagb, njobs=240, util=0.8):
             "host_enqueue_s": st["enqueue_s"], "host_admit_s": st["admit_s"]}
 
 
+# sample-packed layout (64 samples per word): the small-tube and cluster-path
+# configurations, and a wide job of 64 words (4096 samples)
+SP_CASES = [
+    # name, L, Lz, bc, lut, NR, nwords, cadence of one step (itmax, houfr, ptfr, cluster), steps
+    ("L6_Lz24_PBC_NT12_NR2_64samples_ptfr1", 6, 24, 0, "T08_16_N12", 2, 1, (512, 1, 1, False), 8),
+    ("L12_Lz48_OBC_NT24_NR4_64samples_houfr10", 12, 48, 1, "T07_16_N24", 4, 1, (10, 10, 1, True), 10),
+    ("L12_Lz48_OBC_NT24_NR4_4096samples_houfr10", 12, 48, 1, "T07_16_N24", 4, 64, (2, 10, 1, True), 10),
+]
+
+
+def run_sp(args, dev, torch, eagb):
+    """Sample-packed jobs: device-timed spin updates per ps over whole bins
+    (sweeps, tempering every sweep, Houdayer moves, energy measurements)."""
+    out = []
+    for name, Lx, Lz, bc, ln, NR, nw, (itmax, houfr, ptfr, cl), steps in SP_CASES:
+        d = np.load(os.path.join(ROOT, "tests", "golden", "lut_%s.npz" % ln))
+        job = eagb.SpJob(Lx, Lz, d["betas"], d["cum"], nrep=NR, nwords=nw, bc=bc, seeds=MASTERS, device=dev)
+        st = torch.cuda.ExternalStream(job.stream(), device=dev)
+        cad = dict(itmax=itmax, houfr=houfr, mesfr=1, ptfr=ptfr, cluster=cl)
+        for _ in range(max(1, args.warmup)):
+            job.run_async(**cad)
+        job.sync()
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(st)
+        for _ in range(steps):
+            job.run_async(**cad)
+        t1.record(st)
+        job.sync()
+        ms = t0.elapsed_time(t1)
+        V = Lx * Lx * Lz
+        sweeps = steps * itmax * houfr * ptfr
+        su = sweeps * V * NR * len(d["betas"]) * 64 * nw
+        ncol, kt = job.info()
+        out.append({"workload": name, "value": su / (ms * 1e-3) / 1e12, "unit": "spin-updates/ps",
+                    "sweeps": sweeps, "ms": ms, "us_per_sweep": 1e3 * ms / sweeps, "colours": ncol, "tile": kt,
+                    "samples": 64 * nw, "graph": "one bin iteration replayed as a CUDA graph",
+                    "l2": "job of %.1f MB" % (V * NR * len(d["betas"]) * nw * 8 / 1e6)})
+        job.close()
+    return out
+
+
 def run_ours(args, rank, world, local):
     import torch
     eagb = load_eagb()
@@ -435,6 +476,8 @@ def run_ours(args, rank, world, local):
         line["batched"] = [run_mixed(args, dev, torch, eagb, 4, 8), run_mixed(args, dev, torch, eagb, 32, 1)]
     if not args.no_serve:
         line["serving"] = run_serve(args, dev, eagb)
+    if not args.no_sp:
+        line["sample_packed"] = run_sp(args, dev, torch, eagb)
     if not args.no_cpu:
         su, dt = cpu_sample(os.cpu_count() or 1, sweeps=20)
         line["cpu_baseline"] = {"value": su / dt / 1e12, "unit": "spin-updates/ps", "cores": os.cpu_count(),
@@ -455,6 +498,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the batched vs plain mixed-geometry leg")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving (Poisson stream) leg")
+    ap.add_argument("--no-sp", action="store_true", help="skip the sample-packed legs")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -85,22 +85,32 @@ __global__ void __launch_bounds__(512) k_sp_pass(const __grid_constant__ SpDev d
     s_rnd[2 * plane + t] = ((u64)w[4] << 32) | w[5];
   }
   __syncthreads();
+  // Update phase.  A thread keeps one (replica, slot) column (lg) for the
+  // whole loop -- its three random words stay in registers per site -- and
+  // walks (site of the tile, sample word) with a stride of nth/G groups, so
+  // the G lanes of a group touch the G consecutive words of one site.
   const int G = NR * NB;
   const size_t wps = (size_t)V * G;  // words per sample word
-  const int total = kt * d.nw * G;
-  for (int i = tid; i < total; i += nth) {
-    const int b = i % NB, r = (i / NB) % NR, kk = (i / G) % kt, w = i / (G * kt);
-    if (k0 + kk >= n) continue;
-    const int *sn = s_nb + kk * 7;
-    const int site = sn[0];
-    u64 *Sw = d.S + (size_t)w * wps + r * NB + b;
-    const u64 *Jp = d.J + ((size_t)w * V + site) * 6;
-    const u64 sv = Sw[(size_t)site * G];
-    u64 f[6];
+  const int nk = min(kt, n - k0), nidx = nk * d.nw;
+  for (int lg = tid % G, grp = tid / G, ngrp = max(1, nth / G); lg < G; lg += (nth >= G ? G : nth)) {
+    if (nth >= G && grp >= ngrp) break;
+    const int b = lg % NB, r = lg / NB;
+    u64 *Sc = d.S + lg;
+    const int step = nth >= G ? ngrp : 1;
+    int idx = nth >= G ? grp : 0, kk = idx % nk, w = idx / nk;
+    for (; idx < nidx; idx += step) {
+      const int *sn = s_nb + kk * 7;
+      const int site = sn[0];
+      u64 *Sw = Sc + (size_t)w * wps;
+      const u64 *Jp = d.J + ((size_t)w * V + site) * 6;
+      const u64 sv = Sw[(size_t)site * G];
+      u64 f[6];
 #pragma unroll
-    for (int q = 0; q < 6; ++q) f[q] = sv ^ __ldg(Jp + q) ^ Sw[(size_t)sn[q + 1] * G];
-    const int o = (b * kt + kk) * NR + r;
-    Sw[(size_t)site * G] = sv ^ flip_mask(f, s_rnd[o], s_rnd[plane + o], s_rnd[2 * plane + o]);
+      for (int q = 0; q < 6; ++q) f[q] = sv ^ __ldg(Jp + q) ^ Sw[(size_t)sn[q + 1] * G];
+      const int o = (b * kt + kk) * NR + r;
+      Sw[(size_t)site * G] = sv ^ flip_mask(f, s_rnd[o], s_rnd[plane + o], s_rnd[2 * plane + o]);
+      for (kk += step; kk >= nk; kk -= nk) ++w;
+    }
   }
 }
 
@@ -112,12 +122,20 @@ __global__ void __launch_bounds__(512) k_sp_pass(const __grid_constant__ SpDev d
 // bit-sliced counters (one bit plane per power of two, all 64 samples at
 // once), then adds its per-sample totals to U2.
 // ---------------------------------------------------------------------------
-constexpr int kSpChunk = 256;  // sites per thread: 6 * 256 < 2^11
+constexpr int kSpChunkMax = 256;  // sites per thread: 6 * 256 < 2^11
 constexpr int kSpPlanes = 11;
 
-__global__ void __launch_bounds__(256) k_sp_energy(const __grid_constant__ SpDev d) {
+// Sites per thread of the energy kernel: enough threads to fill the GPU
+// (152 SMs x 2048), at least 8 sites each.
+static int sp_energy_chunk(const SpDev &d) {
+  const double words = (double)d.nw * d.V * d.NR * d.NB;
+  int c = (int)(words / (152.0 * 2048.0));
+  return c < 8 ? 8 : (c > kSpChunkMax ? kSpChunkMax : c);
+}
+
+__global__ void __launch_bounds__(256) k_sp_energy(const __grid_constant__ SpDev d, int chunk) {
   const int G = d.NR * d.NB, V = d.V;
-  const int nchunk = (V + kSpChunk - 1) / kSpChunk;
+  const int nchunk = (V + chunk - 1) / chunk;
   const long long col = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // over nw * nchunk * G
   if (col >= (long long)d.nw * nchunk * G) return;
   const int rb = (int)(col % G), ch = (int)((col / G) % nchunk), w = (int)(col / ((long long)G * nchunk));
@@ -126,7 +144,7 @@ __global__ void __launch_bounds__(256) k_sp_energy(const __grid_constant__ SpDev
   u64 P[kSpPlanes];
 #pragma unroll
   for (int p = 0; p < kSpPlanes; ++p) P[p] = 0;
-  const int i0 = ch * kSpChunk, i1 = min(V, i0 + kSpChunk);
+  const int i0 = ch * chunk, i1 = min(V, i0 + chunk);
   for (int i = i0; i < i1; ++i) {
     const u64 sv = Sw[(size_t)i * G];
     const int *nb = d.nb + (size_t)i * 6;
@@ -155,10 +173,11 @@ __global__ void __launch_bounds__(256) k_sp_energy(const __grid_constant__ SpDev
     }
   }
   int32_t *U = d.U2 + (size_t)w * 64 * G + rb;
+  int np = kSpPlanes;
+  while (np > 1 && !P[np - 1]) --np;
   for (int lane = 0; lane < 64; ++lane) {
     int cnt = 0;
-#pragma unroll
-    for (int p = 0; p < kSpPlanes; ++p) cnt |= (int)((P[p] >> lane) & 1ull) << p;
+    for (int p = 0; p < np; ++p) cnt |= (int)((P[p] >> lane) & 1ull) << p;
     if (cnt) atomicAdd(U + (size_t)lane * G, cnt);
   }
 }
@@ -219,24 +238,38 @@ __global__ void __launch_bounds__(64) k_sp_pt(const __grid_constant__ SpDev d) {
 
 // The accepted swaps of the last tempering step, applied to the words in
 // pair order: slot i exchanges the masked samples with slot i+1, and is final
-// after that (one carry word per thread).  Thread per (word, site, replica).
-__global__ void k_sp_permute(const __grid_constant__ SpDev d) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t == 0) *d.ptstep += 1ull;
+// after that (one carry word).  A block stages kPermRows consecutive
+// (word, site, replica) rows of NB words through SMEM, so that global loads
+// and stores are coalesced, and each thread then walks one row.
+constexpr int kPermRows = 128;
+
+__global__ void __launch_bounds__(kPermRows) k_sp_permute(const __grid_constant__ SpDev d) {
+  extern __shared__ u64 rows[];
   const int NB = d.NB, NR = d.NR;
-  if (t >= (long long)d.nw * d.V * NR) return;
-  const int r = (int)(t % NR), w = (int)(t / ((long long)NR * d.V));
-  u64 *p = d.S + (size_t)t * NB;
-  const u64 *M = d.M + ((size_t)w * NR + r) * (NB - 1);
-  u64 cur = p[0];
-  for (int i = 0; i < NB - 1; ++i) {
-    const u64 m = __ldg(M + i);
-    u64 nxt = p[i + 1];
-    const u64 x = (cur ^ nxt) & m;
-    p[i] = cur ^ x;
-    cur = nxt ^ x;
+  const long long nrows = (long long)d.nw * d.V * NR;
+  const long long r0 = (long long)blockIdx.x * kPermRows;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *d.ptstep += 1ull;
+  const int nr = (int)min((long long)kPermRows, nrows - r0);
+  u64 *g = d.S + (size_t)r0 * NB;
+  for (int k = threadIdx.x; k < nr * NB; k += blockDim.x) rows[k] = g[k];
+  __syncthreads();
+  if (threadIdx.x < nr) {
+    const long long t = r0 + threadIdx.x;
+    const int r = (int)(t % NR), w = (int)(t / ((long long)NR * d.V));
+    u64 *p = rows + (size_t)threadIdx.x * NB;
+    const u64 *M = d.M + ((size_t)w * NR + r) * (NB - 1);
+    u64 cur = p[0];
+    for (int i = 0; i < NB - 1; ++i) {
+      const u64 m = __ldg(M + i);
+      const u64 nxt = p[i + 1];
+      const u64 x = (cur ^ nxt) & m;
+      p[i] = cur ^ x;
+      cur = nxt ^ x;
+    }
+    p[NB - 1] = cur;
   }
-  p[NB - 1] = cur;
+  __syncthreads();
+  for (int k = threadIdx.x; k < nr * NB; k += blockDim.x) g[k] = rows[k];
 }
 
 __global__ void k_sp_measure(const __grid_constant__ SpDev d) {
@@ -286,70 +319,96 @@ __global__ void k_sp_overlap(const __grid_constant__ SpDev d, int g) {
   d.Q[t] = p[(size_t)r1 * d.NB] ^ p[(size_t)r2 * d.NB];
 }
 
-__device__ __forceinline__ uint32_t sp_find(const uint32_t *lab, uint32_t x) {
-  uint32_t y = lab[x];
-  while (y != x) { x = y; y = lab[x]; }
-  return x;
-}
-
-// One CTA per (word, slot, sample) lattice: labels in SMEM, atomicMin hooking
-// of roots (a root only ever points to a smaller index, so each cluster ends
-// at its smallest site) until a round joins nothing, then the flips.
+// One CTA per (word, slot, group of 8 samples): the CTA reads its byte of
+// every site's overlap word into SMEM and labels the 8 samples' lattices one
+// after the other with lock-step rounds -- each site hooks the labels of its
+// equal-q neighbours of smaller index with atomicMin, then labels are
+// pointer-jumped until stable, until a round hooks nothing.  Labels only
+// decrease and stay inside the cluster, so each cluster ends labelled by its
+// smallest site.  The roots' coins give the samples' flip bits, gathered per
+// site in a byte that replaces the CTA's byte of the overlap word (the 8
+// groups of a word own disjoint bytes, so no atomics); k_sp_flip then applies
+// the flip words to both replicas.
 __global__ void __launch_bounds__(1024) k_sp_cluster(const __grid_constant__ SpDev d, int g, unsigned long long key) {
   extern __shared__ uint32_t sm[];
-  const int V = d.V, nc = d.nclust, nq = (V + 31) / 32;
-  uint32_t *lab = sm, *qb = sm + V, *sel = qb + nq;
-  const int lane = blockIdx.x & 63, lat = blockIdx.x >> 6;  // lat = w * nc + b
+  const int V = d.V, nc = d.nclust;
+  uint32_t *lab = sm;                                                // [V]
+  uint8_t *qb = reinterpret_cast<uint8_t *>(lab + V);                // [V] q bits of the 8 samples
+  uint8_t *fb = qb + V;                                              // [V] flip bits of the 8 samples
+  uint8_t *bond = fb + V;                                            // [V] equal-q slots to smaller sites
+  const int grp = blockIdx.x & 7, lat = blockIdx.x >> 3;             // lat = w * nc + b
   const int b = lat % nc, w = lat / nc;
-  const u64 *Q = d.Q + (size_t)lat * V;
-  for (int i0 = threadIdx.x & ~31; i0 < nq * 32; i0 += blockDim.x) {
-    const int i = i0 + (threadIdx.x & 31);
-    const unsigned bit = i < V ? (unsigned)((Q[i] >> lane) & 1ull) : 0u;
-    const unsigned m = __ballot_sync(0xffffffffu, bit);
-    if ((threadIdx.x & 31) == 0) qb[i0 >> 5] = m;
+  uint8_t *Qb = reinterpret_cast<uint8_t *>(d.Q + (size_t)lat * V) + grp;
+  for (int i = threadIdx.x; i < V; i += blockDim.x) {
+    qb[i] = Qb[(size_t)i * 8];
+    fb[i] = 0;
   }
-  for (int i = threadIdx.x; i < V; i += blockDim.x) lab[i] = (uint32_t)i;
-  for (int i = threadIdx.x; i < nq; i += blockDim.x) sel[i] = 0;
   __syncthreads();
-  for (;;) {
-    int changed = 0;
+  const unsigned long long mv = *d.move;
+  for (int l = 0; l < 8; ++l) {
     for (int i = threadIdx.x; i < V; i += blockDim.x) {
-      const unsigned qi = (qb[i >> 5] >> (i & 31)) & 1u;
+      const unsigned qi = (qb[i] >> l) & 1u;
+      unsigned m = 0;
 #pragma unroll
       for (int q = 0; q < 6; ++q) {
         const int p = __ldg(d.nb + (size_t)i * 6 + q);
-        if (p < i && ((qb[p >> 5] >> (p & 31)) & 1u) == qi) {
-          const uint32_t a = sp_find(lab, (uint32_t)i), c = sp_find(lab, (uint32_t)p);
-          if (a != c) {
-            atomicMin(&lab[max(a, c)], min(a, c));
-            changed = 1;
+        if (p < i && ((qb[p] >> l) & 1u) == qi) m |= 1u << q;
+      }
+      bond[i] = (uint8_t)m;
+      lab[i] = (uint32_t)i;
+    }
+    __syncthreads();
+    for (;;) {
+      int hooked = 0;
+      for (int i = threadIdx.x; i < V; i += blockDim.x) {
+        const unsigned m = bond[i];
+        if (!m) continue;
+        const uint32_t li = lab[i];
+#pragma unroll
+        for (int q = 0; q < 6; ++q)
+          if ((m >> q) & 1u) {
+            const uint32_t lj = lab[__ldg(d.nb + (size_t)i * 6 + q)];
+            if (lj != li) { atomicMin(&lab[max(li, lj)], min(li, lj)); hooked = 1; }
           }
+      }
+      if (!__syncthreads_or(hooked)) break;
+      for (;;) {
+        int moved = 0;
+        for (int i = threadIdx.x; i < V; i += blockDim.x) {
+          const uint32_t x = lab[i], y = lab[x];
+          if (y != x) { lab[i] = y; moved = 1; }
         }
+        if (!__syncthreads_or(moved)) break;
       }
     }
-    if (!__syncthreads_or(changed)) break;
-  }
-  for (int i = threadIdx.x; i < V; i += blockDim.x) lab[i] = sp_find(lab, (uint32_t)i);
-  __syncthreads();
-  const unsigned long long mv = *d.move;
-  const uint32_t tag = (((uint32_t)(w * 64 + lane) << 6 | (uint32_t)b) << 1) | (uint32_t)g;
-  for (int i = threadIdx.x; i < V; i += blockDim.x) {
-    if (lab[i] != (uint32_t)i) continue;
-    uint32_t v0 = (uint32_t)mv, v1 = (uint32_t)(mv >> 32), v2 = (uint32_t)i, v3 = tag;
-    philox10(v0, v1, v2, v3, (uint32_t)key, (uint32_t)(key >> 32));
-    if (v0 & 1u) atomicOr(&sel[i >> 5], 1u << (i & 31));
-  }
-  __syncthreads();
-  const int r1 = d.pairs[2 * g], r2 = d.pairs[2 * g + 1];
-  const u64 bitw = 1ull << lane;
-  for (int i = threadIdx.x; i < V; i += blockDim.x) {
-    const uint32_t r = lab[i];
-    if ((sel[r >> 5] >> (r & 31)) & 1u) {
-      u64 *p = d.S + (((size_t)w * V + i) * d.NR) * d.NB + b;
-      atomicXor(p + (size_t)r1 * d.NB, bitw);
-      atomicXor(p + (size_t)r2 * d.NB, bitw);
+    // coins of the roots, kept in the roots' bond bytes (no longer needed)
+    const int lane = grp * 8 + l;
+    const uint32_t tag = (((uint32_t)(w * 64 + lane) << 6 | (uint32_t)b) << 1) | (uint32_t)g;
+    for (int i = threadIdx.x; i < V; i += blockDim.x) {
+      if (lab[i] != (uint32_t)i) continue;
+      uint32_t v0 = (uint32_t)mv, v1 = (uint32_t)(mv >> 32), v2 = (uint32_t)i, v3 = tag;
+      philox10(v0, v1, v2, v3, (uint32_t)key, (uint32_t)(key >> 32));
+      bond[i] = (uint8_t)(v0 & 1u);
     }
+    __syncthreads();
+    for (int i = threadIdx.x; i < V; i += blockDim.x) fb[i] |= (uint8_t)(bond[lab[i]] << l);
+    __syncthreads();
   }
+  for (int i = threadIdx.x; i < V; i += blockDim.x) Qb[(size_t)i * 8] = fb[i];
+}
+
+// Both replicas of the group take the flip words: thread per (word, site, slot).
+__global__ void k_sp_flip(const __grid_constant__ SpDev d, int g) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int V = d.V, nc = d.nclust;
+  if (t >= (long long)d.nw * V * nc) return;
+  const int b = (int)(t % nc), i = (int)((t / nc) % V), w = (int)(t / ((long long)nc * V));
+  const u64 F = d.Q[((size_t)w * nc + b) * V + i];
+  if (!F) return;
+  const int r1 = d.pairs[2 * g], r2 = d.pairs[2 * g + 1];
+  u64 *p = d.S + (((size_t)w * V + i) * d.NR) * d.NB + b;
+  p[(size_t)r1 * d.NB] ^= F;
+  p[(size_t)r2 * d.NB] ^= F;
 }
 
 // Energy measurement of a bin's iteration: avgE += 3V - U2 (slot order).
@@ -459,6 +518,8 @@ cudaError_t sp_setup() {
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_sp_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)sp_cluster_smem(kSpClusterMaxV));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_sp_permute, cudaFuncAttributeMaxDynamicSharedMemorySize, kPermRows * 64 * 8);
   return e;
 }
 
@@ -476,8 +537,9 @@ cudaError_t sp_launch_energy(const SpDev &d, cudaStream_t st) {
   const int G = d.NR * d.NB;
   cudaError_t e = cudaMemsetAsync(d.U2, 0, sizeof(int32_t) * (size_t)d.nw * 64 * G, st);
   if (e != cudaSuccess) return e;
-  const long long n = (long long)d.nw * ((d.V + kSpChunk - 1) / kSpChunk) * G;
-  k_sp_energy<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d);
+  const int chunk = sp_energy_chunk(d);
+  const long long n = (long long)d.nw * ((d.V + chunk - 1) / chunk) * G;
+  k_sp_energy<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d, chunk);
   return cudaGetLastError();
 }
 
@@ -488,7 +550,7 @@ cudaError_t sp_launch_pt(const SpDev &d, cudaStream_t st) {
 
 cudaError_t sp_launch_permute(const SpDev &d, cudaStream_t st) {
   const long long n = (long long)d.nw * d.V * d.NR;
-  k_sp_permute<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d);
+  k_sp_permute<<<(unsigned)((n + kPermRows - 1) / kPermRows), kPermRows, (size_t)kPermRows * d.NB * 8, st>>>(d);
   return cudaGetLastError();
 }
 
@@ -498,7 +560,7 @@ cudaError_t sp_launch_measure(const SpDev &d, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-size_t sp_cluster_smem(int V) { return ((size_t)V + 2 * (size_t)((V + 31) / 32)) * 4; }
+size_t sp_cluster_smem(int V) { return (size_t)V * 7; }
 
 cudaError_t sp_launch_houdayer(const SpDev &d, cudaStream_t st) {
   k_sp_pairs<<<1, 32, 0, st>>>(d);
@@ -507,7 +569,8 @@ cudaError_t sp_launch_houdayer(const SpDev &d, cudaStream_t st) {
   for (int g = 0; g < ng; ++g) {
     const long long n = (long long)d.nw * d.nclust * d.V;
     k_sp_overlap<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d, g);
-    k_sp_cluster<<<(unsigned)(d.nw * d.nclust * 64), 1024, sp_cluster_smem(d.V), st>>>(d, g, key);
+    k_sp_cluster<<<(unsigned)(d.nw * d.nclust * 8), 1024, sp_cluster_smem(d.V), st>>>(d, g, key);
+    k_sp_flip<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d, g);
   }
   return cudaGetLastError();
 }
@@ -567,6 +630,11 @@ struct ea_sp {
   std::vector<int32_t> expoff;
   double *exptab = nullptr;
   bool have_temps = false;
+  // one iteration of the bin cadence, replayed as a CUDA graph
+  cudaGraphExec_t it_graph = nullptr;
+  ea_cadence it_cad{};
+  int q_cap = 0;  // slots the overlap buffer holds
+  SpDev it_dev{};  // the descriptor the graph was captured with
 };
 
 namespace {
@@ -673,6 +741,7 @@ int ea_sp_destroy(ea_sp *c) {
   if (c->exptab) cudaFree(c->exptab);
   if (c->d.dos) cudaFree(c->d.dos);
   if (c->d.Q) cudaFree(c->d.Q);
+  if (c->it_graph) cudaGraphExecDestroy(c->it_graph);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
   return EA_OK;
@@ -877,20 +946,28 @@ int ea_sp_get_tempering(ea_sp *c, int32_t *E, uint8_t *perm, uint32_t *acc, uint
   return EA_OK;
 }
 
-static int sp_houdayer(ea_sp *c, int nclust) {
+// Overlap buffer for moves on nclust slots (allocated before any capture).
+static int sp_cluster_prepare(ea_sp *c, int &nclust) {
   SpDev &d = c->d;
   if (d.NR < 2) return spfail(EA_ERR_ARG, "the Houdayer move needs 2 replicas");
   if (d.V > kSpClusterMaxV) return spfail(EA_ERR_ARG, "cluster moves need V <= %d sites (V = %d)", kSpClusterMaxV, d.V);
   if (nclust <= 0) nclust = (int)std::lround(0.5 * d.NB);
   if (nclust > d.NB) nclust = d.NB;
-  if (nclust > d.nclust) {
+  if (nclust > c->q_cap) {
     SCU(cudaStreamSynchronize(c->st));
     if (d.Q) cudaFree(d.Q);
     d.Q = nullptr;
     SCU(cudaMalloc((void **)&d.Q, sizeof(unsigned long long) * (size_t)d.nw * nclust * d.V));
+    c->q_cap = nclust;
   }
   d.nclust = nclust;
-  SCU(sp_launch_houdayer(d, c->st));
+  return EA_OK;
+}
+
+static int sp_houdayer(ea_sp *c, int nclust) {
+  const int rc = sp_cluster_prepare(c, nclust);
+  if (rc) return rc;
+  SCU(sp_launch_houdayer(c->d, c->st));
   return EA_OK;
 }
 
@@ -908,15 +985,42 @@ int ea_sp_run(ea_sp *c, const ea_cadence *cad, double *avgE) {
   const SpDev &d = c->d;
   const size_t n = (size_t)d.nw * 64 * d.NR * d.NB;
   SCU(cudaMemsetAsync(d.avgE, 0, n * 8, c->st));
-  int rc;
-  for (int it = 0; it < cad->itmax; ++it) {
+  int rc, nclust = cad->nclust;
+  if (cad->cluster && (rc = sp_cluster_prepare(c, nclust))) return rc;
+  // one iteration: every launch reads its counters (pass, tempering step,
+  // move) from the device, so the captured graph replays each iteration
+  auto iteration = [&]() -> int {
     for (int im = 0; im < cad->mesfr; ++im) {
-      for (int ih = 0; ih < cad->houfr; ++ih)
-        if ((rc = sp_sweeps(c, cad->ptfr)) || (rc = sp_pt(c))) return rc;
-      if (cad->cluster && (rc = sp_houdayer(c, cad->nclust))) return rc;
+      for (int ih = 0; ih < cad->houfr; ++ih) {
+        int r = sp_sweeps(c, cad->ptfr);
+        if (!r) r = sp_pt(c);
+        if (r) return r;
+      }
+      if (cad->cluster) SCU(sp_launch_houdayer(c->d, c->st));
     }
     SCU(sp_launch_energy(c->d, c->st));
     SCU(sp_launch_measure_u2(c->d, c->st));
+    return EA_OK;
+  };
+  if (cad->itmax == 1) {
+    if ((rc = iteration())) return rc;
+  } else {
+    if (!c->it_graph || std::memcmp(&c->it_cad, cad, sizeof(ea_cadence)) ||
+        std::memcmp(&c->it_dev, &c->d, sizeof(SpDev))) {
+      if (c->it_graph) { cudaGraphExecDestroy(c->it_graph); c->it_graph = nullptr; }
+      cudaGraph_t graph = nullptr;
+      SCU(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+      rc = iteration();
+      const cudaError_t e = cudaStreamEndCapture(c->st, &graph);
+      if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
+      SCU(e);
+      const cudaError_t ei = cudaGraphInstantiate(&c->it_graph, graph, 0);
+      cudaGraphDestroy(graph);
+      SCU(ei);
+      c->it_cad = *cad;
+      c->it_dev = c->d;
+    }
+    for (int it = 0; it < cad->itmax; ++it) SCU(cudaGraphLaunch(c->it_graph, c->st));
   }
   if (avgE) {
     std::vector<double> h(n);

@@ -71,7 +71,8 @@ struct SpDev {
   unsigned long long *dos;           // [nw][64][6V+1] states per energy (E = -3V..3V)
 };
 
-// Largest lattice of the one-CTA cluster labelling (labels in SMEM).
+// Largest lattice of the one-CTA cluster labelling (7 bytes of SMEM per
+// site: label, 8 samples' overlap and flip bits, bond mask).
 constexpr int kSpClusterMaxV = 32768;
 
 int sp_kt(int NB, int NR, int nsites_colour);

@@ -39,7 +39,7 @@ CONFIGS = [
 ]
 
 # temperature sets of the mixed-geometry (batched vs plain) and serving workloads
-EXTRA_LUTS = ["T07_16_N16", "T07_16_N24", "T07_16_N32", "T07_16_N8", "T07_16_N12"]
+EXTRA_LUTS = ["T07_16_N16", "T07_16_N24", "T07_16_N32", "T07_16_N8", "T07_16_N12", "T08_16_N12"]
 
 
 def beta_set(name):
