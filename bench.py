@@ -246,18 +246,34 @@ def serve_stream(njobs, seed=7):
     return jobs
 
 
-def run_serve(args, dev, eagb, njobs=240, util=0.8):
-    """Continuous batching server under a Poisson stream of jobs: p50/p99
-    completion latency and spin-updates/ps of the completed work."""
+# the same stream shape with the sample-packed layout, which takes every
+# L in 6..20: 64 samples per job, NR=4, sweeps log-uniform in 2^6..2^12 (the
+# 2^14..2^20 range scaled by 1/256), in bins of 10 sweeps
+SERVE_SP_WORKLOAD = "poisson_L6-20_LzL1-16_PBC-OBC_NT8-32_NR4_64samples_houfr10_sweeps2^6-2^12"
+
+
+def serve_sp_stream(njobs, seed=9):
+    rng = np.random.default_rng(seed)
+    jobs = []
+    for k in range(njobs):
+        L = int(rng.integers(6, 21))
+        Lz = L * int(rng.choice([1, 2, 4, 8, 16]))
+        bc = int(rng.integers(0, 2))
+        nt = int(rng.choice(SERVE_NT))
+        sweeps = int(round(2.0 ** rng.uniform(6, 12)))
+        jobs.append((L, Lz, bc, nt, max(1, int(round(sweeps / 10.0)))))
+    return jobs
+
+
+def run_serve_stream(dev, eagb, stream, sweeps_per_bin, submit_kw, su_of, capacity, util, workload, seed):
+    """A Poisson stream of jobs through a server: p50/p99 completion latency
+    and spin-updates/ps of the completed work."""
     import threading
-    stream = serve_stream(njobs)
     luts = {nt: np.load(os.path.join(ROOT, "tests", "golden", "lut_T07_16_N%d.npz" % nt)) for nt in SERVE_NT}
-    su = [20 * nb * L * L * Lz * SERVE_NR * nt * SERVE_NS for (L, Lz, bc, nt, nb) in stream]
-    # arrival rate: the stream's work at ~0.6 spin-updates/ps, offered at `util`
-    mean_s = np.mean(su) / 0.6e12
-    rate = util / mean_s
-    rng = np.random.default_rng(11)
-    gaps = rng.exponential(1.0 / rate, size=njobs)
+    njobs = len(stream)
+    su = [su_of(*j) for j in stream]
+    rate = util / (np.mean(su) / capacity)
+    gaps = np.random.default_rng(seed).exponential(1.0 / rate, size=njobs)
     srv = eagb.Server(device=dev, nb_max=32, depth=2)
     tickets = [None] * njobs
     err = []
@@ -271,8 +287,8 @@ def run_serve(args, dev, eagb, njobs=240, util=0.8):
                 if t > d:
                     time.sleep(t - d)
                 m = tuple((x ^ (0x9E3779B97F4A7C15 * (k + 1))) & 0xFFFFFFFFFFFFFFFF or 1 for x in MASTERS)
-                tickets[k] = srv.submit(L, Lz, luts[nt]["betas"], luts[nt]["cum"], SERVE_NS, SERVE_NR, bc, m, nb,
-                                        itmax=2, houfr=10, mesfr=1, ptfr=1, cluster=True, jobid=k & 0x3FFF)
+                tickets[k] = srv.submit(L, Lz, luts[nt]["betas"], luts[nt]["cum"], nbins=nb, masters=m,
+                                        bc=bc, jobid=k & 0x3FFF, **submit_kw)
         except Exception as e:  # reported below
             err.append(e)
 
@@ -300,13 +316,30 @@ def run_serve(args, dev, eagb, njobs=240, util=0.8):
         raise err[0]
     st = srv.stats()
     srv.close()
-    return {"workload": SERVE_WORKLOAD, "jobs": njobs, "arrival_rate_per_s": rate, "offered_load": util,
+    return {"workload": workload, "jobs": njobs, "arrival_rate_per_s": rate, "offered_load": util,
             "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"], "max_ms": st["max_ms"],
             "value": st["spin_updates"] / st["span_s"] / 1e12, "unit": "spin-updates/ps",
             "span_s": st["span_s"], "completed": st["completed"], "failed": st["failed"],
             "peak_running": st["peak_running"], "bins": st["bins"], "batch_changes": st["batch_changes"],
             "hbm_budget": st["budget"], "hbm_peak": st["bytes_peak"], "gpu_busy_s": st["gpu_busy_s"],
             "host_enqueue_s": st["enqueue_s"], "host_admit_s": st["admit_s"]}
+
+
+def run_serve_sp(args, dev, eagb, njobs=100, util=0.8):
+    stream = serve_sp_stream(njobs)
+    kw = dict(nsamples=1, NR=SERVE_NR, itmax=1, houfr=10, mesfr=1, ptfr=1, cluster=True,
+              layout=eagb.EA_LAYOUT_SAMPLE_PACKED, nwords=1)
+    su_of = lambda L, Lz, bc, nt, nb: 10 * nb * L * L * Lz * SERVE_NR * nt * 64
+    return run_serve_stream(dev, eagb, stream, 10, kw, su_of, 0.3e12, util, SERVE_SP_WORKLOAD, 13)
+
+
+def run_serve(args, dev, eagb, njobs=240, util=0.8):
+    """Continuous batching server under a Poisson stream of multispin jobs
+    (batched with their class)."""
+    stream = serve_stream(njobs)
+    kw = dict(nsamples=SERVE_NS, NR=SERVE_NR, itmax=2, houfr=10, mesfr=1, ptfr=1, cluster=True)
+    su_of = lambda L, Lz, bc, nt, nb: 20 * nb * L * L * Lz * SERVE_NR * nt * SERVE_NS
+    return run_serve_stream(dev, eagb, stream, 20, kw, su_of, 0.6e12, util, SERVE_WORKLOAD, 11)
 
 
 # sample-packed layout (64 samples per word): the small-tube and cluster-path
@@ -476,6 +509,7 @@ def run_ours(args, rank, world, local):
         line["batched"] = [run_mixed(args, dev, torch, eagb, 4, 8), run_mixed(args, dev, torch, eagb, 32, 1)]
     if not args.no_serve:
         line["serving"] = run_serve(args, dev, eagb)
+        line["serving_sample_packed"] = run_serve_sp(args, dev, eagb)
     if not args.no_sp:
         line["sample_packed"] = run_sp(args, dev, torch, eagb)
     if not args.no_cpu:

@@ -54,6 +54,7 @@ struct Job {
   std::vector<double> betas;
   std::vector<uint64_t> cum;
   ea_ctx *ctx = nullptr;
+  ea_sp *sp = nullptr;  // sample-packed jobs
   int state = EA_JOB_QUEUED;
   int rc = EA_OK;
   std::string err;
@@ -62,11 +63,16 @@ struct Job {
   uint64_t bytes = 0;
   int passed = 0;  // times a later request was admitted ahead of this one
   bool freeing = false;  // handed to the reaper
+  bool packed() const { return req.layout == EA_LAYOUT_SAMPLE_PACKED; }
+  ea_sp_geom spgeom() const {
+    const ea_geom &g = req.geom;
+    return ea_sp_geom{g.L, g.Lz, g.nbetas, g.nrep, req.nwords, g.bc};
+  }
   double su() const {
     const ea_geom &g = req.geom;
     const ea_cadence &c = req.cad;
-    return (double)req.nbins * c.itmax * c.mesfr * c.houfr * c.ptfr * g.L * g.L * g.Lz * g.nrep * g.nbetas *
-           g.nsamples;
+    const double samples = packed() ? 64.0 * req.nwords : (double)g.nsamples;
+    return (double)req.nbins * c.itmax * c.mesfr * c.houfr * c.ptfr * g.L * g.L * g.Lz * g.nrep * g.nbetas * samples;
   }
 };
 
@@ -78,10 +84,13 @@ struct InFlight {
   std::vector<Job *> finishing;  // jobs whose last bin this is
 };
 
+// A group is a batch of multispin jobs of one class, or one sample-packed
+// job (solo) whose bins run on its own stream.
 struct Group {
   ClassKey key;
   ea_cadence cad{};
   int NR = 0;
+  Job *solo = nullptr;
   ea_batch *batch = nullptr;
   std::vector<Job *> members;
   bool dirty = false;
@@ -181,13 +190,25 @@ void retire(ea_server *s, bool block) {
   }
 }
 
-Group *group_for(ea_server *s, const Job *j) {
+Group *group_for(ea_server *s, Job *j) {
   const ea_cadence &c = j->req.cad;
   const ClassKey key{j->req.geom.nrep, c.itmax, c.houfr, c.mesfr, c.ptfr, c.cluster, c.nclust};
-  for (auto &g : s->groups)
-    if (g->key == key) return g.get();
+  if (!j->packed())
+    for (auto &g : s->groups)
+      if (!g->solo && g->key == key) return g.get();
+  if (j->packed()) {
+    // a finished solo group whose bins have all ended is reused
+    for (auto &g : s->groups)
+      if (g->solo && g->members.empty() && g->inflight.empty()) {
+        g->solo = j;
+        g->cad = c;
+        g->NR = j->req.geom.nrep;
+        return g.get();
+      }
+  }
   s->groups.emplace_back(new Group());
   Group *g = s->groups.back().get();
+  if (j->packed()) g->solo = j;
   g->key = key;
   g->cad = c;
   g->NR = j->req.geom.nrep;
@@ -207,6 +228,20 @@ int tile_for(int NR, int nb_max) {
 
 // Creates and initialises an admitted job's context (worker thread).
 int create_job(ea_server *s, Job *j) {
+  if (j->packed()) {
+    const ea_sp_geom g = j->spgeom();
+    ea_sp *p = nullptr;
+    int rc = ea_sp_create(&g, s->cfg.device, &p);
+    if (rc) return rc;
+    rc = ea_sp_set_temperatures(p, j->betas.data(), j->cum.data());
+    if (!rc) rc = ea_sp_init(p, j->req.masters, j->req.jobid);
+    if (rc) {
+      ea_sp_destroy(p);
+      return rc;
+    }
+    j->sp = p;
+    return EA_OK;
+  }
   ea_ctx *c = nullptr;
   int rc = ea_create(&j->req.geom, s->cfg.device, &c);
   if (rc) return rc;
@@ -317,7 +352,12 @@ bool step_group(ea_server *s, Group *g) {
   f.ev0 = get_event(s);
   std::vector<ea_ctx *> ctxs;
   for (Job *j : g->members) ctxs.push_back(j->ctx);
-  if (!g->batch) {
+  void *st = nullptr;
+  if (g->solo) {
+    ea_sp_stream(g->solo->sp, &st);
+    cudaEventRecord(f.ev0, (cudaStream_t)st);
+    rc = ea_sp_run(g->solo->sp, &g->cad, nullptr);
+  } else if (!g->batch) {
     rc = ea_batch_create(ctxs.data(), (int32_t)ctxs.size(), s->cfg.tile ? s->cfg.tile : tile_for(g->NR, s->cfg.nb_max),
                          &g->batch);
     if (rc == EA_OK) ++s->changes;
@@ -325,8 +365,7 @@ bool step_group(ea_server *s, Group *g) {
     rc = ea_batch_set_jobs(g->batch, ctxs.data(), (int32_t)ctxs.size());
     if (rc == EA_OK) ++s->changes;
   }
-  void *st = nullptr;
-  if (rc == EA_OK) {
+  if (rc == EA_OK && !g->solo) {
     g->dirty = false;
     ea_batch_stream(g->batch, &st);
     cudaEventRecord(f.ev0, (cudaStream_t)st);
@@ -366,6 +405,7 @@ bool step_group(ea_server *s, Group *g) {
   if (!f.finishing.empty()) {
     g->members = stay;
     g->dirty = true;
+    if (g->solo && stay.empty()) g->solo = nullptr;
   }
   g->inflight.push_back(std::move(f));
   return true;
@@ -437,9 +477,12 @@ void reaper_main(ea_server *s) {
     Job *j = s->to_free.front();
     s->to_free.pop_front();
     ea_ctx *c = j->ctx;
+    ea_sp *p = j->sp;
     j->ctx = nullptr;
+    j->sp = nullptr;
     lk.unlock();
     if (c) ea_destroy(c);
+    if (p) ea_sp_destroy(p);
     lk.lock();
     j->state = EA_JOB_RELEASED;
     s->in_use -= j->bytes;
@@ -482,9 +525,21 @@ int ea_server_submit(ea_server *s, const ea_request *r, int64_t *ticket) {
   if (r->nbins < 1 || r->cad.itmax < 1 || r->cad.houfr < 1 || r->cad.mesfr < 1 || r->cad.ptfr < 0)
     return sfail(EA_ERR_ARG, "bad cadence or bin count");
   if (g.nbetas > s->cfg.nb_max) return sfail(EA_ERR_ARG, "NB=%d above the server's nb_max=%d", g.nbetas, s->cfg.nb_max);
-  if (r->cad.cluster && g.nrep < 4) return sfail(EA_ERR_ARG, "the Houdayer move needs at least 2 replicas per group");
+  if (r->cad.cluster && g.nrep < (r->layout == EA_LAYOUT_SAMPLE_PACKED ? 2 : 4))
+    return sfail(EA_ERR_ARG, "the Houdayer move needs at least 2 replicas per group");
+  if (r->layout == EA_LAYOUT_SAMPLE_PACKED && (r->cad.ptfr < 1 || r->cad.nclust > g.nbetas))
+    return sfail(EA_ERR_ARG, "sample-packed jobs temper every ptfr >= 1 sweeps");
   std::unique_ptr<Job> j(new Job());
-  int rc = ea_job_bytes(&g, &r->cad, r->betas, &j->bytes);
+  int rc;
+  if (r->layout == EA_LAYOUT_SAMPLE_PACKED) {
+    if (r->nwords < 1) return sfail(EA_ERR_ARG, "a sample-packed job needs nwords >= 1");
+    const ea_sp_geom sg{g.L, g.Lz, g.nbetas, g.nrep, r->nwords, g.bc};
+    rc = ea_sp_job_bytes(&sg, &r->cad, r->betas, &j->bytes);
+  } else if (r->layout == EA_LAYOUT_MULTISPIN) {
+    rc = ea_job_bytes(&g, &r->cad, r->betas, &j->bytes);
+  } else {
+    return sfail(EA_ERR_ARG, "unknown layout %d", r->layout);
+  }
   if (rc) return sfail(rc, "%s", ea_last_error());
   std::lock_guard<std::mutex> lk(s->m);
   if (s->stop) return sfail(EA_ERR_STATE, "server is shutting down");
@@ -537,6 +592,17 @@ int ea_server_info(ea_server *s, int64_t ticket, ea_job_info *info) {
   info->t_done = j->t_done;
   info->bytes = j->bytes;
   info->spin_updates = j->su();
+  return EA_OK;
+}
+
+int ea_server_sp_job(ea_server *s, int64_t ticket, ea_sp **job) {
+  if (!s || !job) return sfail(EA_ERR_ARG, "null argument");
+  std::lock_guard<std::mutex> lk(s->m);
+  auto it = s->jobs.find(ticket);
+  if (it == s->jobs.end()) return sfail(EA_ERR_ARG, "unknown ticket %lld", (long long)ticket);
+  const Job *j = it->second.get();
+  if (j->state != EA_JOB_DONE || !j->sp) return sfail(EA_ERR_STATE, "job %lld is not a finished sample-packed job", (long long)ticket);
+  *job = j->sp;
   return EA_OK;
 }
 
@@ -625,7 +691,7 @@ int ea_server_destroy(ea_server *s) {
   {
     std::lock_guard<std::mutex> lk(s->m);
     for (auto &kv : s->jobs)
-      if (kv.second->ctx && !kv.second->freeing) {
+      if ((kv.second->ctx || kv.second->sp) && !kv.second->freeing) {
         kv.second->freeing = true;
         s->to_free.push_back(kv.second.get());
       }

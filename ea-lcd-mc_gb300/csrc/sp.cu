@@ -329,10 +329,13 @@ __global__ void k_sp_overlap(const __grid_constant__ SpDev d, int g) {
 // site in a byte that replaces the CTA's byte of the overlap word (the 8
 // groups of a word own disjoint bytes, so no atomics); k_sp_flip then applies
 // the flip words to both replicas.
+// Lattices above kSpClusterMaxV sites keep the same arrays in a global
+// scratch region of the CTA (L2-resident) instead of SMEM.
 __global__ void __launch_bounds__(1024) k_sp_cluster(const __grid_constant__ SpDev d, int g, unsigned long long key) {
   extern __shared__ uint32_t sm[];
   const int V = d.V, nc = d.nclust;
-  uint32_t *lab = sm;                                                // [V]
+  uint32_t *base = V <= kSpClusterMaxV ? sm : d.cscratch + (size_t)blockIdx.x * sp_cluster_words(V);
+  uint32_t *lab = base;                                              // [V]
   uint8_t *qb = reinterpret_cast<uint8_t *>(lab + V);                // [V] q bits of the 8 samples
   uint8_t *fb = qb + V;                                              // [V] flip bits of the 8 samples
   uint8_t *bond = fb + V;                                            // [V] equal-q slots to smaller sites
@@ -394,6 +397,7 @@ __global__ void __launch_bounds__(1024) k_sp_cluster(const __grid_constant__ SpD
     for (int i = threadIdx.x; i < V; i += blockDim.x) fb[i] |= (uint8_t)(bond[lab[i]] << l);
     __syncthreads();
   }
+  __syncthreads();
   for (int i = threadIdx.x; i < V; i += blockDim.x) Qb[(size_t)i * 8] = fb[i];
 }
 
@@ -560,7 +564,7 @@ cudaError_t sp_launch_measure(const SpDev &d, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-size_t sp_cluster_smem(int V) { return (size_t)V * 7; }
+size_t sp_cluster_smem(int V) { return V <= kSpClusterMaxV ? (size_t)V * 7 : 0; }
 
 cudaError_t sp_launch_houdayer(const SpDev &d, cudaStream_t st) {
   k_sp_pairs<<<1, 32, 0, st>>>(d);
@@ -741,6 +745,7 @@ int ea_sp_destroy(ea_sp *c) {
   if (c->exptab) cudaFree(c->exptab);
   if (c->d.dos) cudaFree(c->d.dos);
   if (c->d.Q) cudaFree(c->d.Q);
+  if (c->d.cscratch) cudaFree(c->d.cscratch);
   if (c->it_graph) cudaGraphExecDestroy(c->it_graph);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
@@ -950,14 +955,17 @@ int ea_sp_get_tempering(ea_sp *c, int32_t *E, uint8_t *perm, uint32_t *acc, uint
 static int sp_cluster_prepare(ea_sp *c, int &nclust) {
   SpDev &d = c->d;
   if (d.NR < 2) return spfail(EA_ERR_ARG, "the Houdayer move needs 2 replicas");
-  if (d.V > kSpClusterMaxV) return spfail(EA_ERR_ARG, "cluster moves need V <= %d sites (V = %d)", kSpClusterMaxV, d.V);
   if (nclust <= 0) nclust = (int)std::lround(0.5 * d.NB);
   if (nclust > d.NB) nclust = d.NB;
   if (nclust > c->q_cap) {
     SCU(cudaStreamSynchronize(c->st));
     if (d.Q) cudaFree(d.Q);
+    if (d.cscratch) cudaFree(d.cscratch);
     d.Q = nullptr;
+    d.cscratch = nullptr;
     SCU(cudaMalloc((void **)&d.Q, sizeof(unsigned long long) * (size_t)d.nw * nclust * d.V));
+    if (d.V > kSpClusterMaxV)
+      SCU(cudaMalloc((void **)&d.cscratch, sizeof(uint32_t) * sp_cluster_words(d.V) * (size_t)d.nw * nclust * 8));
     c->q_cap = nclust;
   }
   d.nclust = nclust;
@@ -1028,6 +1036,40 @@ int ea_sp_run(ea_sp *c, const ea_cadence *cad, double *avgE) {
     SCU(cudaStreamSynchronize(c->st));
     for (size_t i = 0; i < n; ++i) avgE[i] = h[i] / cad->itmax;
   }
+  return EA_OK;
+}
+
+int ea_sp_job_bytes(const ea_sp_geom *gp, const ea_cadence *cad, const double *betas, uint64_t *bytes) {
+  SpGraph g;
+  if (!bytes || !geom_ok(gp) || !sp_graph(gp->L, gp->Lz, gp->bc, g)) return spfail(EA_ERR_ARG, "bad sample-packed geometry");
+  uint64_t tot = 0;
+  auto add = [&](uint64_t n) {
+    n = std::max<uint64_t>(n, 1);
+    tot += n >= (1ull << 20) ? (n + (2ull << 20) - 1) & ~((2ull << 20) - 1) : (n + 511) & ~(uint64_t)511;
+  };
+  const uint64_t V = g.V, NB = gp->nbetas, NR = gp->nrep, nw = gp->nwords, G = NR * NB;
+  add(V * 24); add(V * 4);                                   // neighbour table, colour lists
+  add(nw * V * G * 8); add(nw * V * 48);                     // spins, couplings
+  add(NB * 256 * 8); add(NB * 256 * 2);                      // thresholds, pre-search
+  add(NR * 16); add(NR * 4); add(NR * sizeof(ea_hq)); add(NR * sizeof(ea_xoshiro)); add(8);
+  add(nw * 64 * G * 4); add(nw * 64 * G * 4); add(nw * 64 * G);   // U2, E, slot permutations
+  add(nw * 64 * NR * (NB - 1) * 4); add(nw * NR * (NB - 1) * 8); // accepted swaps, lane masks
+  add(NB * 8); add(NB * 4); add(8); add(nw * 64 * G * 8);   // betas, exp offsets, step, averages
+  add(sizeof(ea_hq)); add(16); add(8);                      // random_c, pairs, move counter
+  uint64_t nexp = (NB - 1) * 25001;
+  if (betas) {
+    std::vector<double> tab;
+    std::vector<int32_t> off;
+    pt_exp_table(betas, (int)NB, tab, off);
+    nexp = tab.size();
+  }
+  add(nexp * 8);
+  if (cad && cad->cluster) {
+    const uint64_t nc = (uint64_t)(cad->nclust > 0 ? std::min<int>(cad->nclust, (int)NB) : std::lround(0.5 * NB));
+    add(nw * nc * V * 8);
+    if (V > (uint64_t)kSpClusterMaxV) add(nw * nc * 8 * sp_cluster_words((int)V) * 4);
+  }
+  *bytes = tot + (2ull << 20);                               // stream, graph, small-allocation pages
   return EA_OK;
 }
 

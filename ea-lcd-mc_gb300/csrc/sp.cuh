@@ -67,13 +67,16 @@ struct SpDev {
   unsigned long long *Q;             // [nw][nclust][V] overlap words s_r1 ^ s_r2
   unsigned long long *move;          // cluster moves so far
   int nclust;
+  uint32_t *cscratch;                // labelling arrays of lattices above kSpClusterMaxV, per CTA
   // exact enumeration
   unsigned long long *dos;           // [nw][64][6V+1] states per energy (E = -3V..3V)
 };
 
-// Largest lattice of the one-CTA cluster labelling (7 bytes of SMEM per
-// site: label, 8 samples' overlap and flip bits, bond mask).
+// Largest lattice of the one-CTA cluster labelling in SMEM (7 bytes per
+// site: label, 8 samples' overlap and flip bits, bond mask); larger ones use
+// a global scratch region of sp_cluster_words(V) words per CTA.
 constexpr int kSpClusterMaxV = 32768;
+__host__ __device__ inline size_t sp_cluster_words(int V) { return ((size_t)V * 7 + 15) / 16 * 4; }
 
 int sp_kt(int NB, int NR, int nsites_colour);
 size_t sp_sweep_smem(int NB, int NR, int kt);

@@ -45,9 +45,13 @@ class ServerConfig(C.Structure):
                 ("nb_max", C.c_int32), ("reserved", C.c_int32), ("hbm_budget", C.c_uint64)]
 
 
+EA_LAYOUT_MULTISPIN, EA_LAYOUT_SAMPLE_PACKED = 0, 1
+
+
 class Request(C.Structure):
     _fields_ = [("geom", Geom), ("betas", C.c_void_p), ("cum", C.c_void_p), ("masters", C.c_uint64 * 4),
-                ("cad", Cadence), ("nbins", C.c_int32), ("jobid", C.c_uint32), ("iter0", C.c_int64)]
+                ("cad", Cadence), ("nbins", C.c_int32), ("jobid", C.c_uint32), ("iter0", C.c_int64),
+                ("layout", C.c_int32), ("nwords", C.c_int32)]
 
 
 class JobInfo(C.Structure):
@@ -382,19 +386,28 @@ class Server:
         self.s = C.c_void_p()
         _ck(lib().ea_server_create(C.byref(cfg), C.byref(self.s)))
         self._geoms = {}
-        self._keep = {}
+        self._sp_geom = {}
 
     def submit(self, L, Lz, betas, cum, nsamples, NR, bc, masters, nbins, itmax, houfr, mesfr, ptfr,
-               cluster=True, nclust=0, jobid=0, iter0=0):
+               cluster=True, nclust=0, jobid=0, iter0=0, layout=EA_LAYOUT_MULTISPIN, nwords=1):
         betas = np.ascontiguousarray(betas, np.float64)
         cum = np.ascontiguousarray(cum, np.uint64)
         g = geom(L, Lz, len(betas), NR, nsamples, bc)
         r = Request(g, betas.ctypes.data, cum.ctypes.data, (C.c_uint64 * 4)(*[int(x) for x in masters]),
-                    Cadence(itmax, houfr, mesfr, ptfr, int(cluster), nclust), nbins, jobid, iter0)
+                    Cadence(itmax, houfr, mesfr, ptfr, int(cluster), nclust), nbins, jobid, iter0, layout, nwords)
         t = C.c_int64()
         _ck(lib().ea_server_submit(self.s, C.byref(r), C.byref(t)))
         self._geoms[t.value] = g
+        if layout == EA_LAYOUT_SAMPLE_PACKED:
+            self._sp_geom[t.value] = (SpGeom(L, Lz, len(betas), NR, nwords, bc), betas)
         return t.value
+
+    def sp_job(self, ticket):
+        """View of a finished sample-packed job (owned by the server)."""
+        h = C.c_void_p()
+        _ck(lib().ea_server_sp_job(self.s, C.c_int64(ticket), C.byref(h)))
+        g, betas = self._sp_geom[ticket]
+        return SpView(g, betas, h)
 
     def wait(self, ticket, timeout=-1.0):
         ctx = C.c_void_p()
@@ -548,3 +561,16 @@ class SpJob:
         mean = np.zeros((ns, len(b)))
         _ck(lib().ea_sp_exact(self.h, P(b), len(b), P(dos), P(mean)))
         return dos, mean
+
+
+class SpView(SpJob):
+    """A sample-packed job owned by someone else (a server): no create/destroy."""
+
+    def __init__(self, g, betas, handle):
+        self.g = g
+        self.V = g.L * g.L * g.Lz
+        self.betas = betas
+        self.h = handle
+
+    def close(self):
+        self.h = None

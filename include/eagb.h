@@ -259,81 +259,6 @@ int ea_init_run(ea_ctx *ctx, const uint64_t masters[4], const int32_t *list_samp
  * charges for it.  betas (may be NULL) sizes the tempering exp table exactly. */
 int ea_job_bytes(const ea_geom *g, const ea_cadence *cad, const double *betas, uint64_t *bytes);
 
-/* ---- serving: continuous batching of simulation jobs -------------------------
- * A server owns one device and a worker thread.  Submitted jobs wait in a
- * queue until their device bytes (ea_job_bytes) fit the HBM budget and a slot
- * is free; admitted jobs are created and initialised as new runs
- * (ea_init_run), join the batch of their replica count and cadence, and are
- * advanced one bin per step by the batched kernels, interleaved with every
- * other running job; a job leaves its batch after its last bin.  Up to
- * `depth` bins per batch are in flight, and the job list of a batch changes
- * between bins without draining the GPU.  Each job's words, energies, swaps
- * and uniforms equal those of the same job run alone by ea_run_bin.  Latency
- * is submission to completion as the worker observes it (host clock).  A
- * finished job's context stays readable (ea_get_spins, ea_bin_results, ...)
- * until ea_server_release.  No reference counterpart: the reference runs one
- * job per process. */
-typedef struct ea_server ea_server;
-typedef struct {
-  int32_t device;
-  int32_t max_jobs;      /* jobs admitted at once (<= 0: 1024) */
-  int32_t depth;         /* bins in flight per batch (<= 0: 2) */
-  int32_t tile;          /* sweep tile width of the batches (0: the widest that fits nb_max) */
-  int32_t nb_max;        /* largest accepted NB (<= 0: 64) */
-  int32_t reserved;
-  uint64_t hbm_budget;   /* device bytes the jobs may hold (0: 90 % of the free memory at creation) */
-} ea_server_config;
-
-typedef struct {
-  ea_geom geom;
-  const double *betas;   /* [nbetas], copied */
-  const uint64_t *cum;   /* [nbetas][256], copied */
-  uint64_t masters[4];   /* seed_J, seed_u, seed_MC, seed_cluster */
-  ea_cadence cad;        /* one bin */
-  int32_t nbins;         /* bins to run (>= 1) */
-  uint32_t jobid;        /* 14-bit Philox job id */
-  int64_t iter0;         /* initial half-sweep counter */
-} ea_request;
-
-enum { EA_JOB_QUEUED = 0, EA_JOB_RUNNING = 1, EA_JOB_DONE = 2, EA_JOB_FAILED = 3, EA_JOB_RELEASED = 4 };
-typedef struct {
-  int32_t state;
-  int32_t bins_done;
-  double t_submit, t_admit, t_done;  /* seconds since the server's creation (-1: not yet) */
-  uint64_t bytes;                    /* charged against the budget */
-  double spin_updates;
-} ea_job_info;
-
-typedef struct {
-  int64_t submitted, admitted, completed, failed, queued, running;
-  int64_t bins, batch_changes, peak_running;
-  double p50_ms, p99_ms, mean_ms, max_ms;  /* completion latency of the completed jobs */
-  double spin_updates;                     /* of the completed jobs */
-  double span_s;                           /* first submission to last completion */
-  uint64_t budget, bytes_in_use, bytes_peak;
-  double gpu_busy_s;  /* sum of the bins' device durations (CUDA events) */
-  double enqueue_s;   /* worker time spent enqueueing bins (batch changes included) */
-  double admit_s;     /* worker time spent creating and initialising admitted jobs */
-} ea_serve_stats;
-
-int ea_server_create(const ea_server_config *cfg, ea_server **out);
-/* Queues a job; returns EA_ERR_ARG for a request that can never run (bad
- * geometry, NB above nb_max, bytes above the budget). */
-int ea_server_submit(ea_server *s, const ea_request *r, int64_t *ticket);
-/* Waits until the job is done or failed (timeout_s < 0: no limit); job (may be
- * NULL) receives its context, still owned by the server.  EA_ERR_STATE on
- * timeout; the job's own error code if it failed. */
-int ea_server_wait(ea_server *s, int64_t ticket, double timeout_s, ea_ctx **job);
-int ea_server_info(ea_server *s, int64_t ticket, ea_job_info *info);
-/* Frees a finished job's device memory (asynchronously; the budget is
- * credited once it is freed). */
-int ea_server_release(ea_server *s, int64_t ticket);
-int ea_server_stats(ea_server *s, ea_serve_stats *st);
-/* Waits until every submitted job has finished. */
-int ea_server_drain(ea_server *s);
-/* Cancels queued jobs, waits for the running ones' bins and frees everything. */
-int ea_server_destroy(ea_server *s);
-
 /* ---- sample-packed layout: any L >= 2, Lz >= 2, any number of replicas -------
  * No reference counterpart: the reference's multispin words hold 64 spatial
  * sub-blocks of one sample, so L and Lz must be multiples of 8
@@ -399,7 +324,8 @@ int ea_sp_get_tempering(ea_sp *job, int32_t *E, uint8_t *perm, uint32_t *acc, ui
  * overlap along all six bond slots (fake bonds included: E(r1)+E(r2) is
  * conserved for any L), smallest-site roots, each cluster flipped in both
  * replicas with probability 1/2 (a Philox bit of move, root, sample, slot,
- * group).  V <= 32768 sites. */
+ * group).  Lattices up to 32768 sites are labelled in shared memory, larger
+ * ones in a device scratch area of 7 bytes per site and labelled lattice. */
 int ea_sp_houdayer(ea_sp *job, int32_t nclust);
 /* One bin of the reference's cadence (main.cu:149-230): itmax x [mesfr x
  * (houfr x (ptfr sweeps + tempering) + Houdayer if cad->cluster) + energy
@@ -410,6 +336,90 @@ int ea_sp_run(ea_sp *job, const ea_cadence *cad, double *avgE);
  * spin 0 up at each E = -3V..3V, and meanE [nwords*64][nbeta] = <E>(beta)
  * from it in FP64 on the GPU. */
 int ea_sp_exact(ea_sp *job, const double *betas, int32_t nbeta, uint64_t *dos, double *meanE);
+/* Upper bound of the device bytes of a sample-packed job after bins of cadence cad (NULL: none). */
+int ea_sp_job_bytes(const ea_sp_geom *g, const ea_cadence *cad, const double *betas, uint64_t *bytes);
+
+/* ---- serving: continuous batching of simulation jobs -------------------------
+ * A server owns one device and a worker thread.  Submitted jobs wait in a
+ * queue until their device bytes (ea_job_bytes) fit the HBM budget and a slot
+ * is free; admitted jobs are created and initialised as new runs
+ * (ea_init_run), join the batch of their replica count and cadence, and are
+ * advanced one bin per step by the batched kernels, interleaved with every
+ * other running job; a job leaves its batch after its last bin.  Up to
+ * `depth` bins per batch are in flight, and the job list of a batch changes
+ * between bins without draining the GPU.  Each job's words, energies, swaps
+ * and uniforms equal those of the same job run alone by ea_run_bin.  Latency
+ * is submission to completion as the worker observes it (host clock).  A
+ * finished job's context stays readable (ea_get_spins, ea_bin_results, ...)
+ * until ea_server_release.  No reference counterpart: the reference runs one
+ * job per process. */
+typedef struct ea_server ea_server;
+typedef struct {
+  int32_t device;
+  int32_t max_jobs;      /* jobs admitted at once (<= 0: 1024) */
+  int32_t depth;         /* bins in flight per batch (<= 0: 2) */
+  int32_t tile;          /* sweep tile width of the batches (0: the widest that fits nb_max) */
+  int32_t nb_max;        /* largest accepted NB (<= 0: 64) */
+  int32_t reserved;
+  uint64_t hbm_budget;   /* device bytes the jobs may hold (0: 90 % of the free memory at creation) */
+} ea_server_config;
+
+enum { EA_LAYOUT_MULTISPIN = 0, EA_LAYOUT_SAMPLE_PACKED = 1 };
+typedef struct {
+  ea_geom geom;          /* sample-packed: nsamples unused, see nwords */
+  const double *betas;   /* [nbetas], copied */
+  const uint64_t *cum;   /* [nbetas][256], copied */
+  uint64_t masters[4];   /* multispin: seed_J, seed_u, seed_MC, seed_cluster; sample-packed: ea_sp_init's seeds */
+  ea_cadence cad;        /* one bin */
+  int32_t nbins;         /* bins to run (>= 1) */
+  uint32_t jobid;        /* 14-bit Philox job id */
+  int64_t iter0;         /* initial half-sweep counter (multispin) */
+  int32_t layout;        /* EA_LAYOUT_MULTISPIN: batched with its class; EA_LAYOUT_SAMPLE_PACKED:
+                            any L, Lz >= 2, bins on the job's own stream */
+  int32_t nwords;        /* sample-packed: words of 64 samples */
+} ea_request;
+
+enum { EA_JOB_QUEUED = 0, EA_JOB_RUNNING = 1, EA_JOB_DONE = 2, EA_JOB_FAILED = 3, EA_JOB_RELEASED = 4 };
+typedef struct {
+  int32_t state;
+  int32_t bins_done;
+  double t_submit, t_admit, t_done;  /* seconds since the server's creation (-1: not yet) */
+  uint64_t bytes;                    /* charged against the budget */
+  double spin_updates;
+} ea_job_info;
+
+typedef struct {
+  int64_t submitted, admitted, completed, failed, queued, running;
+  int64_t bins, batch_changes, peak_running;
+  double p50_ms, p99_ms, mean_ms, max_ms;  /* completion latency of the completed jobs */
+  double spin_updates;                     /* of the completed jobs */
+  double span_s;                           /* first submission to last completion */
+  uint64_t budget, bytes_in_use, bytes_peak;
+  double gpu_busy_s;  /* sum of the bins' device durations (CUDA events) */
+  double enqueue_s;   /* worker time spent enqueueing bins (batch changes included) */
+  double admit_s;     /* worker time spent creating and initialising admitted jobs */
+} ea_serve_stats;
+
+int ea_server_create(const ea_server_config *cfg, ea_server **out);
+/* Queues a job; returns EA_ERR_ARG for a request that can never run (bad
+ * geometry, NB above nb_max, bytes above the budget). */
+int ea_server_submit(ea_server *s, const ea_request *r, int64_t *ticket);
+/* Waits until the job is done or failed (timeout_s < 0: no limit); job (may be
+ * NULL) receives its context, still owned by the server.  EA_ERR_STATE on
+ * timeout; the job's own error code if it failed. */
+int ea_server_wait(ea_server *s, int64_t ticket, double timeout_s, ea_ctx **job);
+int ea_server_info(ea_server *s, int64_t ticket, ea_job_info *info);
+/* The sample-packed job of a finished request (ea_server_wait's job is NULL for those). */
+int ea_server_sp_job(ea_server *s, int64_t ticket, ea_sp **job);
+/* Frees a finished job's device memory (asynchronously; the budget is
+ * credited once it is freed). */
+int ea_server_release(ea_server *s, int64_t ticket);
+int ea_server_stats(ea_server *s, ea_serve_stats *st);
+/* Waits until every submitted job has finished. */
+int ea_server_drain(ea_server *s);
+/* Cancels queued jobs, waits for the running ones' bins and frees everything. */
+int ea_server_destroy(ea_server *s);
+
 
 /* cuRAND XORWOW uniforms (device generator) for a seed/offset, copied to host.
  * Used to check the device generator against the host one. */

@@ -182,3 +182,51 @@ def test_budget_and_rejection():
     st = srv.stats()
     srv.close()
     assert st["completed"] == 3 and st["peak_running"] == 1
+
+
+SP_JOBS = [
+    # L, Lz, lut, bc, nwords, NR, nbins, cadence (itmax, houfr, mesfr, ptfr, cluster)
+    (5, 10, "T07_16_N6", O.PBC, 1, 4, 3, (2, 2, 1, 1, 1)),
+    (7, 14, "T07_16_N8", O.OBC, 2, 2, 2, (3, 1, 1, 1, 0)),
+    (6, 6, "T08_16_N4", O.OBC, 1, 4, 4, (1, 3, 1, 1, 1)),
+]
+
+
+def sp_alone(k):
+    L, Lz, ln, bc, nw, NR, nbins, (itmax, houfr, mesfr, ptfr, cl) = SP_JOBS[k]
+    betas, cum = lut(ln)
+    job = eagb.SpJob(L, Lz, betas, cum, nrep=NR, nwords=nw, bc=bc, seeds=masters(50 + k), jobid=200 + k)
+    for _ in range(nbins):
+        avg = job.run_bin(itmax, houfr, mesfr, ptfr, cluster=bool(cl))
+    return job, avg
+
+
+@pytest.mark.gpu
+def test_served_sample_packed_jobs_equal_jobs_alone():
+    """Sample-packed jobs of odd and even L served next to multispin jobs:
+    each ends exactly as the same job run alone."""
+    srv = eagb.Server(max_jobs=8, depth=2)
+    tickets = []
+    for k in range(len(SP_JOBS)):
+        L, Lz, ln, bc, nw, NR, nbins, (itmax, houfr, mesfr, ptfr, cl) = SP_JOBS[k]
+        betas, cum = lut(ln)
+        tickets.append(srv.submit(L, Lz, betas, cum, 1, NR, bc, masters(50 + k), nbins, itmax, houfr, mesfr, ptfr,
+                                  cluster=bool(cl), jobid=200 + k, layout=eagb.EA_LAYOUT_SAMPLE_PACKED, nwords=nw))
+        if k == 0:
+            tickets.append(submit(srv, 0))   # a multispin job in the mix
+    for t in tickets:
+        srv.wait(t, timeout=60.0)
+    k = 0
+    for t in tickets:
+        if t in srv._sp_geom:
+            served = srv.sp_job(t)
+            alone, avg = sp_alone(k)
+            assert np.array_equal(served.get_spins(), alone.get_spins()), "sample-packed job %d" % k
+            assert all(np.array_equal(a, b) for a, b in zip(served.tempering(), alone.tempering()))
+            assert served.counter() == alone.counter()
+            alone.close()
+            k += 1
+        srv.release(t)
+    st = srv.stats()
+    srv.close()
+    assert st["completed"] == len(tickets) and st["failed"] == 0
