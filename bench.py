@@ -31,6 +31,9 @@ L, LZ, NR, NS, HOUFR = 24, 192, 8, 31, 5
 LUT = os.path.join(ROOT, "tests", "golden", "lut_T06_16_N32.npz")
 MASTERS = (0x1234567890ABCDEF, 0x0FEDCBA987654321, 0x1111222233334444, 0x5555666677778888)
 WORKLOAD = "L24_Lz192_OBC_NB32_NR8_ns31_ptfr1_houfr5"
+# DRAM bytes (read + write) of one k_sweep launch of this workload, from an
+# ncu capture (mean of two launches)
+KSWEEP_DRAM_BYTES = 136.0e6
 # mixed-geometry workload of the batched vs plain comparison: every
 # L x (Lz/L) x boundary x NT combination is one job class
 # (36 geometry classes; either 36 jobs of 32 samples or 288 jobs of 4)
@@ -357,6 +360,10 @@ def run_sp(args, dev, torch, eagb):
     (sweeps, tempering every sweep, Houdayer moves, energy measurements)."""
     out = []
     for name, Lx, Lz, bc, ln, NR, nw, (itmax, houfr, ptfr, cl), steps in SP_CASES:
+        if args.sp_case and args.sp_case not in name:
+            continue
+        if args.sp_case:
+            steps = args.steps
         d = np.load(os.path.join(ROOT, "tests", "golden", "lut_%s.npz" % ln))
         job = eagb.SpJob(Lx, Lz, d["betas"], d["cum"], nrep=NR, nwords=nw, bc=bc, seeds=MASTERS, device=dev)
         st = torch.cuda.ExternalStream(job.stream(), device=dev)
@@ -499,7 +506,9 @@ def run_ours(args, rank, world, local):
                 "d2h_bytes_per_step": NS * NR * NB * 4},
         "gpu_launches": args.steps * (HOUFR * 6 + 1 + 2 * 4 + 3),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": None, "kernel": "k_sweep", "peak_kind": how,
+                     "traffic": KSWEEP_DRAM_BYTES, "traffic_source": "ncu dram__bytes_read+write per k_sweep launch "
+                     "of this workload (profiles/k_sweep_dram_bench_L24_Lz192_NB32_ns31.md)",
+                     "kernel": "k_sweep", "peak_kind": how,
                      "alg_bytes_per_launch": alg_bytes, "launch_ms": sweep_ms, "launches": nsw.value},
         "kernel_ms": {"sweep": sw_ms.value, "pt": pt_ms.value, "cluster": cl_ms.value,
                       "uniforms_overlapped": rg_ms.value, "step_total": ms},
@@ -533,6 +542,8 @@ def main():
     ap.add_argument("--no-mixed", action="store_true", help="skip the batched vs plain mixed-geometry leg")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving (Poisson stream) leg")
     ap.add_argument("--no-sp", action="store_true", help="skip the sample-packed legs")
+    ap.add_argument("--sp-case", default="", help="run only the sample-packed workloads whose name contains this "
+                    "(--steps bins after --warmup; prints their JSON records)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -542,6 +553,9 @@ def main():
         torch.distributed.init_process_group("nccl" if args.impl == "ours" else "gloo")
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.sp_case:
+        import torch
+        print(json.dumps(run_sp(args, local, torch, load_eagb())), flush=True)
     else:
         run_ours(args, rank, world, local)
     if world > 1:
