@@ -400,6 +400,8 @@ def run_ours(args, rank, world, local):
     NB = len(betas)
     V = L * L * LZ
     job = eagb.new_job(L, LZ, betas, cum, nsamples=NS, NR=NR, bc=eagb.EA_OBC, masters=MASTERS, device=dev, jobid=rank)
+    if args.rng_sms >= 0:
+        job.set_rng_sms(args.rng_sms)
     stream = torch.cuda.ExternalStream(job.stream(), device=dev)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.int32, device=dev)   # 512 MB > L2
     su_step = HOUFR * V * NR * NB * NS
@@ -509,6 +511,7 @@ def run_ours(args, rank, world, local):
                      "traffic": KSWEEP_DRAM_BYTES, "traffic_source": "ncu dram__bytes_read+write per k_sweep launch "
                      "of this workload (profiles/k_sweep_dram_bench_L24_Lz192_NB32_ns31.md)",
                      "kernel": "k_sweep", "peak_kind": how,
+                     "binding_pipe": "integer ALU: 58.4 % of peak in ncu (profiles/k_sweep_full_bench_L24_Lz192_NB32_ns31.md)",
                      "alg_bytes_per_launch": alg_bytes, "launch_ms": sweep_ms, "launches": nsw.value},
         "kernel_ms": {"sweep": sw_ms.value, "pt": pt_ms.value, "cluster": cl_ms.value,
                       "uniforms_overlapped": rg_ms.value, "step_total": ms},
@@ -542,6 +545,8 @@ def main():
     ap.add_argument("--no-mixed", action="store_true", help="skip the batched vs plain mixed-geometry leg")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving (Poisson stream) leg")
     ap.add_argument("--no-sp", action="store_true", help="skip the sample-packed legs")
+    ap.add_argument("--rng-sms", type=int, default=-1,
+                    help="SMs of the cluster-uniform generator's partition for the headline job (-1: automatic)")
     ap.add_argument("--sp-case", default="", help="run only the sample-packed workloads whose name contains this "
                     "(--steps bins after --warmup; prints their JSON records)")
     args = ap.parse_args()
