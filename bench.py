@@ -390,6 +390,82 @@ def run_sp(args, dev, torch, eagb):
     return out
 
 
+# batching configuration with the sample-packed layout: every L x (Lz/L) x
+# boundary x NT class of L in {8,10,12,16}, Lz/L in {2,4,8}, NT in
+# {16,24,32} (72 classes) as one job; 4096 sample words (262,144 samples) in
+# all, NR=2, a Houdayer move every 10 sweeps
+SPMIX_L, SPMIX_RATIO, SPMIX_NT, SPMIX_WORDS, SPMIX_NR = (8, 10, 12, 16), (2, 4, 8), (16, 24, 32), 4096, 2
+SPMIX_WORKLOAD = "mixed_L8-16_Lz2-8L_PBC-OBC_NT16-32_NR2_%dwords_houfr10"
+
+
+def spmix_jobs(eagb, dev, nwords):
+    classes = [(L, r * L, bc, nt) for L in SPMIX_L for r in SPMIX_RATIO for bc in (0, 1) for nt in SPMIX_NT]
+    words = [nwords // len(classes) + (1 if k < nwords % len(classes) else 0) for k in range(len(classes))]
+    jobs = []
+    for k, ((L, Lz, bc, nt), nw) in enumerate(zip(classes, words)):
+        d = np.load(os.path.join(ROOT, "tests", "golden", "lut_T07_16_N%d.npz" % nt))
+        m = tuple((x ^ (0x9E3779B97F4A7C15 * (k + 1))) & 0xFFFFFFFFFFFFFFFF or 1 for x in MASTERS)
+        jobs.append(eagb.SpJob(L, Lz, d["betas"], d["cum"], nrep=SPMIX_NR, nwords=nw, bc=bc, seeds=m, jobid=k,
+                               device=dev))
+    return jobs
+
+
+def run_mixed_sp(args, dev, torch, eagb, nwords=SPMIX_WORDS, steps=2):
+    """Sample-packed batching: one bin (10 sweeps + tempering each sweep, one
+    Houdayer move, a measurement) of every class job, plain (one job per
+    launch sequence, each on its own stream, all enqueued before waiting) vs
+    batched (one launch per kernel kind for all 72 jobs), from twin states."""
+    plain, batched = spmix_jobs(eagb, dev, nwords), spmix_jobs(eagb, dev, nwords)
+    batch = eagb.SpBatch(batched)
+    cad = dict(itmax=1, houfr=10, mesfr=1, ptfr=1, cluster=True)
+    su_step = sum(10 * j.V * SPMIX_NR * j.g.nbetas * 64 * j.g.nwords for j in plain)
+    spin_bytes = sum(8.0 * j.V * SPMIX_NR * j.g.nbetas * j.g.nwords for j in plain)
+    s0 = torch.cuda.Stream(device=dev)
+
+    def timed(streams_of, enqueue, n):
+        streams = [torch.cuda.ExternalStream(h, device=dev) for h in streams_of]
+        torch.cuda.synchronize(dev)
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(s0)
+        for st in streams:
+            st.wait_event(t0)
+        for _ in range(n):
+            enqueue()
+        for st in streams:
+            e = torch.cuda.Event()
+            e.record(st)
+            s0.wait_event(e)
+        t1.record(s0)
+        torch.cuda.synchronize(dev)
+        return t0.elapsed_time(t1)
+
+    def plain_step():
+        for j in plain:
+            j.run_async(**cad)
+
+    def batch_step():
+        batch.run_bin(**cad)
+
+    pstreams = [j.stream() for j in plain]
+    bstreams = [batch.stream()]
+    timed(pstreams, plain_step, 1)
+    timed(bstreams, batch_step, 1)
+    ms_plain = timed(pstreams, plain_step, steps)
+    ms_batch = timed(bstreams, batch_step, steps)
+    same = all(np.array_equal(a.get_spins(), b.get_spins()) for a, b in zip(plain, batched))
+    batch.close()
+    for j in plain + batched:
+        j.close()
+    vp = su_step * steps / (ms_plain * 1e-3) / 1e12
+    vb = su_step * steps / (ms_batch * 1e-3) / 1e12
+    return {"workload": SPMIX_WORKLOAD % nwords, "jobs": len(plain), "samples": 64 * nwords, "unit": "spin-updates/ps",
+            "plain_value": vp, "batched_value": vb, "speedup": vb / vp, "plain_ms_per_step": ms_plain / steps,
+            "batched_ms_per_step": ms_batch / steps, "spin_updates_per_step": su_step,
+            "bit_exact_plain_vs_batched": bool(same),
+            "graph": "one bin iteration of the batch replayed as a CUDA graph",
+            "l2": "spin words %.2f GB against a 129 MB L2" % (spin_bytes / 1e9)}
+
+
 def run_ours(args, rank, world, local):
     import torch
     eagb = load_eagb()
@@ -518,7 +594,8 @@ def run_ours(args, rank, world, local):
         "clocks": clk.summary(),
     }
     if not args.no_mixed:
-        line["batched"] = [run_mixed(args, dev, torch, eagb, 4, 8), run_mixed(args, dev, torch, eagb, 32, 1)]
+        line["batched"] = [run_mixed(args, dev, torch, eagb, 4, 8), run_mixed(args, dev, torch, eagb, 32, 1),
+                           run_mixed_sp(args, dev, torch, eagb), run_mixed_sp(args, dev, torch, eagb, 72, 10)]
     if not args.no_serve:
         line["serving"] = run_serve(args, dev, eagb)
         line["serving_sample_packed"] = run_serve_sp(args, dev, eagb)

@@ -24,7 +24,7 @@ void set_last_error(const char *msg);  // api.cu
 // half-sweep counter (its parity bit = the counter's lowest bit, as for
 // half-sweeps), so every pass of every sweep has its own counters.
 // ---------------------------------------------------------------------------
-__global__ void k_sp_fill(const __grid_constant__ SpDev d) {
+__device__ __forceinline__ void sp_fill_body(const SpDev &d) {
   JobDev j{};
   j.NR = d.NR; j.xo = d.xo; j.prc = d.prc; j.ctr = d.ctr; j.iter = d.iter; j.jobid = d.jobid;
   const int parity = (int)(*d.iter & 1);
@@ -40,15 +40,14 @@ __global__ void k_sp_fill(const __grid_constant__ SpDev d) {
 // consecutive lanes touch consecutive words of a site.  The Philox thread
 // index of (slot b, site i, replica r) is (b*V + i)*NR + r.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(512) k_sp_pass(const __grid_constant__ SpDev d, int off, int n) {
-  extern __shared__ __align__(16) unsigned char smem[];
+__device__ __forceinline__ void sp_pass_body(const SpDev &d, int off, int n, int tile, unsigned char *smem) {
   const int NB = d.NB, NR = d.NR, kt = d.kt, V = d.V;
   u64 *s_cum = reinterpret_cast<u64 *>(smem);
   uint16_t *s_pre = reinterpret_cast<uint16_t *>(s_cum + NB * 256);
   u64 *s_rnd = reinterpret_cast<u64 *>(s_pre + NB * 256);
   int *s_nb = reinterpret_cast<int *>(s_rnd + 3 * NB * kt * NR);  // [kt][7]: site, 6 neighbours
   const int tid = threadIdx.x, nth = blockDim.x;
-  const int k0 = blockIdx.x * kt;
+  const int k0 = tile * kt;
   {
     const uint4 *cs = reinterpret_cast<const uint4 *>(d.cum);
     uint4 *cd = reinterpret_cast<uint4 *>(s_cum);
@@ -127,16 +126,16 @@ constexpr int kSpPlanes = 11;
 
 // Sites per thread of the energy kernel: enough threads to fill the GPU
 // (152 SMs x 2048), at least 8 sites each.
-static int sp_energy_chunk(const SpDev &d) {
+int sp_energy_chunk(const SpDev &d) {
   const double words = (double)d.nw * d.V * d.NR * d.NB;
   int c = (int)(words / (152.0 * 2048.0));
   return c < 8 ? 8 : (c > kSpChunkMax ? kSpChunkMax : c);
 }
 
-__global__ void __launch_bounds__(256) k_sp_energy(const __grid_constant__ SpDev d, int chunk) {
-  const int G = d.NR * d.NB, V = d.V;
+__device__ __forceinline__ void sp_energy_body(const SpDev &d, int blk) {
+  const int G = d.NR * d.NB, V = d.V, chunk = d.echunk;
   const int nchunk = (V + chunk - 1) / chunk;
-  const long long col = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // over nw * nchunk * G
+  const long long col = (long long)blk * blockDim.x + threadIdx.x;  // over nw * nchunk * G
   if (col >= (long long)d.nw * nchunk * G) return;
   const int rb = (int)(col % G), ch = (int)((col / G) % nchunk), w = (int)(col / ((long long)G * nchunk));
   const u64 *Sw = d.S + (size_t)w * V * G + rb;
@@ -193,9 +192,9 @@ __global__ void __launch_bounds__(256) k_sp_energy(const __grid_constant__ SpDev
 // draw replaces the 2 KB of state per chain.  A warp holds 32 samples of one
 // (word, replica): the accepted swaps of pair i form the lane mask M[i].
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(64) k_sp_pt(const __grid_constant__ SpDev d) {
+__device__ __forceinline__ void sp_pt_body(const SpDev &d, int wr) {
   const int NB = d.NB, NR = d.NR, G = NR * NB;
-  const int wr = blockIdx.x, w = wr / NR, r = wr % NR, lane = threadIdx.x;
+  const int w = wr / NR, r = wr % NR, lane = threadIdx.x;
   const int nt = 3 * d.V;
   const size_t o = ((size_t)w * 64 + lane) * G + (size_t)r * NB;
   const unsigned long long step = *d.ptstep;
@@ -243,12 +242,11 @@ __global__ void __launch_bounds__(64) k_sp_pt(const __grid_constant__ SpDev d) {
 // and stores are coalesced, and each thread then walks one row.
 constexpr int kPermRows = 128;
 
-__global__ void __launch_bounds__(kPermRows) k_sp_permute(const __grid_constant__ SpDev d) {
-  extern __shared__ u64 rows[];
+__device__ __forceinline__ void sp_permute_body(const SpDev &d, int blk, u64 *rows) {
   const int NB = d.NB, NR = d.NR;
   const long long nrows = (long long)d.nw * d.V * NR;
-  const long long r0 = (long long)blockIdx.x * kPermRows;
-  if (blockIdx.x == 0 && threadIdx.x == 0) *d.ptstep += 1ull;
+  const long long r0 = (long long)blk * kPermRows;
+  if (blk == 0 && threadIdx.x == 0) *d.ptstep += 1ull;
   const int nr = (int)min((long long)kPermRows, nrows - r0);
   u64 *g = d.S + (size_t)r0 * NB;
   for (int k = threadIdx.x; k < nr * NB; k += blockDim.x) rows[k] = g[k];
@@ -272,10 +270,6 @@ __global__ void __launch_bounds__(kPermRows) k_sp_permute(const __grid_constant_
   for (int k = threadIdx.x; k < nr * NB; k += blockDim.x) g[k] = rows[k];
 }
 
-__global__ void k_sp_measure(const __grid_constant__ SpDev d) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < (long long)d.nw * 64 * d.NR * d.NB) d.avgE[i] += (double)d.E[i];
-}
 
 // ---------------------------------------------------------------------------
 // Houdayer move (main.cu:351-453, HoudayerXEA.cu:54-374), per sample.
@@ -292,8 +286,7 @@ __global__ void k_sp_measure(const __grid_constant__ SpDev d) {
 // (sample, beta, root) with 0.5 (HoudayerXEA.cu:373); a counter-based bit
 // needs no V*NB uniforms per sample.
 // ---------------------------------------------------------------------------
-__global__ void k_sp_pairs(const __grid_constant__ SpDev d) {
-  if (threadIdx.x) return;
+__device__ __forceinline__ void sp_pairs_body(const SpDev &d) {
   *d.move += 1ull;
   const int ng = d.NR >= 4 ? 2 : 1, h = d.NR / ng;
   for (int g = 0; g < ng; ++g) {
@@ -309,8 +302,7 @@ __global__ void k_sp_pairs(const __grid_constant__ SpDev d) {
   }
 }
 
-__global__ void k_sp_overlap(const __grid_constant__ SpDev d, int g) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // (w, b, site)
+__device__ __forceinline__ void sp_overlap_body(const SpDev &d, int g, long long t) {  // t = (w, b, site)
   const int V = d.V, nc = d.nclust;
   if (t >= (long long)d.nw * nc * V) return;
   const int i = (int)(t % V), b = (int)((t / V) % nc), w = (int)(t / ((long long)V * nc));
@@ -331,15 +323,18 @@ __global__ void k_sp_overlap(const __grid_constant__ SpDev d, int g) {
 // the flip words to both replicas.
 // Lattices above kSpClusterMaxV sites keep the same arrays in a global
 // scratch region of the CTA (L2-resident) instead of SMEM.
-__global__ void __launch_bounds__(1024) k_sp_cluster(const __grid_constant__ SpDev d, int g, unsigned long long key) {
-  extern __shared__ uint32_t sm[];
+// Key of the cluster coins of a job: its tempering seed, offset.
+__host__ __device__ inline unsigned long long sp_cluster_key(const SpDev &d) { return d.pt_seed ^ 0xC2B2AE3585EBCA6BULL; }
+
+__device__ __forceinline__ void sp_cluster_body(const SpDev &d, int g, int blk, uint32_t *sm) {
+  const unsigned long long key = sp_cluster_key(d);
   const int V = d.V, nc = d.nclust;
-  uint32_t *base = V <= kSpClusterMaxV ? sm : d.cscratch + (size_t)blockIdx.x * sp_cluster_words(V);
+  uint32_t *base = V <= kSpClusterMaxV ? sm : d.cscratch + (size_t)blk * sp_cluster_words(V);
   uint32_t *lab = base;                                              // [V]
   uint8_t *qb = reinterpret_cast<uint8_t *>(lab + V);                // [V] q bits of the 8 samples
   uint8_t *fb = qb + V;                                              // [V] flip bits of the 8 samples
   uint8_t *bond = fb + V;                                            // [V] equal-q slots to smaller sites
-  const int grp = blockIdx.x & 7, lat = blockIdx.x >> 3;             // lat = w * nc + b
+  const int grp = blk & 7, lat = blk >> 3;                           // lat = w * nc + b
   const int b = lat % nc, w = lat / nc;
   uint8_t *Qb = reinterpret_cast<uint8_t *>(d.Q + (size_t)lat * V) + grp;
   for (int i = threadIdx.x; i < V; i += blockDim.x) {
@@ -402,8 +397,7 @@ __global__ void __launch_bounds__(1024) k_sp_cluster(const __grid_constant__ SpD
 }
 
 // Both replicas of the group take the flip words: thread per (word, site, slot).
-__global__ void k_sp_flip(const __grid_constant__ SpDev d, int g) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void sp_flip_body(const SpDev &d, int g, long long t) {
   const int V = d.V, nc = d.nclust;
   if (t >= (long long)d.nw * V * nc) return;
   const int b = (int)(t % nc), i = (int)((t / nc) % V), w = (int)(t / ((long long)nc * V));
@@ -416,8 +410,7 @@ __global__ void k_sp_flip(const __grid_constant__ SpDev d, int g) {
 }
 
 // Energy measurement of a bin's iteration: avgE += 3V - U2 (slot order).
-__global__ void k_sp_measure_u2(const __grid_constant__ SpDev d) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void sp_measure_u2_body(const SpDev &d, long long i) {
   if (i < (long long)d.nw * 64 * d.NR * d.NB) d.avgE[i] += (double)(3 * d.V - d.U2[i]);
 }
 
@@ -497,6 +490,176 @@ __global__ void k_sp_exact(const __grid_constant__ SpDev d, const double *betas,
 }
 
 // ---------------------------------------------------------------------------
+// Batched kernels: block b works for job j with pre[j] <= b < pre[j+1], on the
+// job's block b - pre[j]; the bodies are the one-job kernels', so a job's
+// words are the same alone and in a batch.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int spb_job(const uint32_t *pre, int n, uint32_t v) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(pre + mid) <= v) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+#define SPB_ITEM(KIND)                                        \
+  const uint32_t *pre_ = b.pre[KIND];                         \
+  const int jb = spb_job(pre_, b.njobs, blockIdx.x);          \
+  const SpDev &d = b.jobs[jb];                                \
+  const int blk = (int)(blockIdx.x - __ldg(pre_ + jb));
+
+__global__ void kb_sp_fill(const __grid_constant__ SpBatchDev b, int colour) {
+  const SpDev &d = b.jobs[blockIdx.x];
+  if (colour < d.ncol) sp_fill_body(d);
+}
+__global__ void __launch_bounds__(512) kb_sp_pass(const __grid_constant__ SpBatchDev b, int colour) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  SPB_ITEM(SPB_PASS0 + colour)
+  sp_pass_body(d, d.col_off[colour], d.col_off[colour + 1] - d.col_off[colour], blk, smem);
+}
+__global__ void kb_sp_zero(const __grid_constant__ SpBatchDev b) {
+  SPB_ITEM(SPB_ZERO)
+  const long long i = (long long)blk * blockDim.x + threadIdx.x;
+  if (i < (long long)d.nw * 64 * d.NR * d.NB) d.U2[i] = 0;
+}
+__global__ void __launch_bounds__(256) kb_sp_energy(const __grid_constant__ SpBatchDev b) {
+  SPB_ITEM(SPB_ENERGY)
+  sp_energy_body(d, blk);
+}
+__global__ void __launch_bounds__(64) kb_sp_pt(const __grid_constant__ SpBatchDev b) {
+  SPB_ITEM(SPB_PT)
+  sp_pt_body(d, blk);
+}
+__global__ void __launch_bounds__(kPermRows) kb_sp_permute(const __grid_constant__ SpBatchDev b) {
+  extern __shared__ u64 rows[];
+  SPB_ITEM(SPB_PERMUTE)
+  sp_permute_body(d, blk, rows);
+}
+__global__ void kb_sp_measure(const __grid_constant__ SpBatchDev b) {
+  SPB_ITEM(SPB_MEASURE)
+  sp_measure_u2_body(d, (long long)blk * blockDim.x + threadIdx.x);
+}
+__global__ void kb_sp_pairs(const __grid_constant__ SpBatchDev b) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < b.njobs && b.jobs[j].nclust > 0) sp_pairs_body(b.jobs[j]);
+}
+__global__ void kb_sp_overlap(const __grid_constant__ SpBatchDev b, int g) {
+  SPB_ITEM(SPB_OVL0 + g)
+  sp_overlap_body(d, g, (long long)blk * blockDim.x + threadIdx.x);
+}
+__global__ void __launch_bounds__(1024) kb_sp_cluster(const __grid_constant__ SpBatchDev b, int g) {
+  extern __shared__ uint32_t sm[];
+  SPB_ITEM(SPB_CL0 + g)
+  sp_cluster_body(d, g, blk, sm);
+}
+__global__ void kb_sp_flip(const __grid_constant__ SpBatchDev b, int g) {
+  SPB_ITEM(SPB_FL0 + g)
+  sp_flip_body(d, g, (long long)blk * blockDim.x + threadIdx.x);
+}
+
+size_t sp_cluster_smem(int V);
+
+// Blocks of job d for each batched kernel kind (the one-job launch geometry).
+void sp_batch_blocks(const SpDev &d, bool cluster, uint32_t out[SPB_COUNT]) {
+  const long long G = (long long)d.NR * d.NB, nw = d.nw;
+  for (int k = 0; k < SPB_COUNT; ++k) out[k] = 0;
+  for (int c = 0; c < kSpBatchMaxColours && c < d.ncol; ++c)
+    out[SPB_PASS0 + c] = (uint32_t)((d.col_off[c + 1] - d.col_off[c] + d.kt - 1) / d.kt);
+  out[SPB_ZERO] = out[SPB_MEASURE] = (uint32_t)((nw * 64 * G + 255) / 256);
+  out[SPB_ENERGY] = (uint32_t)((nw * ((d.V + d.echunk - 1) / d.echunk) * G + 255) / 256);
+  out[SPB_PT] = (uint32_t)(nw * d.NR);
+  out[SPB_PERMUTE] = (uint32_t)((nw * d.V * d.NR + kPermRows - 1) / kPermRows);
+  if (cluster && d.nclust > 0) {
+    const int ng = d.NR >= 4 ? 2 : 1;
+    for (int g = 0; g < ng; ++g) {
+      out[SPB_OVL0 + g] = out[SPB_FL0 + g] = (uint32_t)((nw * d.nclust * d.V + 255) / 256);
+      out[SPB_CL0 + g] = (uint32_t)(nw * d.nclust * 8);
+    }
+  }
+}
+
+cudaError_t sp_batch_setup() {
+  cudaError_t e = cudaFuncSetAttribute(kb_sp_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(kb_sp_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sp_cluster_smem(kSpClusterMaxV));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(kb_sp_permute, cudaFuncAttributeMaxDynamicSharedMemorySize, kPermRows * 64 * 8);
+  return e;
+}
+
+// One sweep of every job: colour by colour, each job's counters advanced only
+// for the colours it has.
+cudaError_t sp_batch_sweep(const SpBatchDev &b, int ncol_max, cudaStream_t st) {
+  for (int c = 0; c < ncol_max; ++c) {
+    kb_sp_fill<<<b.njobs, 64, 0, st>>>(b, c);
+    if (b.total[SPB_PASS0 + c]) kb_sp_pass<<<b.total[SPB_PASS0 + c], 512, b.pass_smem, st>>>(b, c);
+  }
+  return cudaGetLastError();
+}
+
+static void spb_energy(const SpBatchDev &b, cudaStream_t st) {
+  kb_sp_zero<<<b.total[SPB_ZERO], 256, 0, st>>>(b);
+  kb_sp_energy<<<b.total[SPB_ENERGY], 256, 0, st>>>(b);
+}
+
+cudaError_t sp_batch_tempering(const SpBatchDev &b, cudaStream_t st) {
+  spb_energy(b, st);
+  kb_sp_pt<<<b.total[SPB_PT], 64, 0, st>>>(b);
+  kb_sp_permute<<<b.total[SPB_PERMUTE], kPermRows, b.perm_smem, st>>>(b);
+  return cudaGetLastError();
+}
+
+cudaError_t sp_batch_houdayer(const SpBatchDev &b, cudaStream_t st) {
+  kb_sp_pairs<<<(b.njobs + 127) / 128, 128, 0, st>>>(b);
+  for (int g = 0; g < 2; ++g) {
+    if (!b.total[SPB_CL0 + g]) continue;
+    kb_sp_overlap<<<b.total[SPB_OVL0 + g], 256, 0, st>>>(b, g);
+    kb_sp_cluster<<<b.total[SPB_CL0 + g], b.cluster_threads, b.cluster_smem, st>>>(b, g);
+    kb_sp_flip<<<b.total[SPB_FL0 + g], 256, 0, st>>>(b, g);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t sp_batch_measure(const SpBatchDev &b, cudaStream_t st) {
+  spb_energy(b, st);
+  kb_sp_measure<<<b.total[SPB_MEASURE], 256, 0, st>>>(b);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// One-job kernels: the bodies above, one block per item
+// ---------------------------------------------------------------------------
+__global__ void k_sp_fill(const __grid_constant__ SpDev d) { sp_fill_body(d); }
+__global__ void __launch_bounds__(512) k_sp_pass(const __grid_constant__ SpDev d, int off, int n) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  sp_pass_body(d, off, n, blockIdx.x, smem);
+}
+__global__ void __launch_bounds__(256) k_sp_energy(const __grid_constant__ SpDev d) { sp_energy_body(d, blockIdx.x); }
+__global__ void __launch_bounds__(64) k_sp_pt(const __grid_constant__ SpDev d) { sp_pt_body(d, blockIdx.x); }
+__global__ void __launch_bounds__(kPermRows) k_sp_permute(const __grid_constant__ SpDev d) {
+  extern __shared__ u64 rows[];
+  sp_permute_body(d, blockIdx.x, rows);
+}
+__global__ void k_sp_pairs(const __grid_constant__ SpDev d) {
+  if (threadIdx.x == 0) sp_pairs_body(d);
+}
+__global__ void k_sp_overlap(const __grid_constant__ SpDev d, int g) {
+  sp_overlap_body(d, g, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
+__global__ void __launch_bounds__(1024) k_sp_cluster(const __grid_constant__ SpDev d, int g) {
+  extern __shared__ uint32_t sm[];
+  sp_cluster_body(d, g, blockIdx.x, sm);
+}
+__global__ void k_sp_flip(const __grid_constant__ SpDev d, int g) {
+  sp_flip_body(d, g, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
+__global__ void k_sp_measure_u2(const __grid_constant__ SpDev d) {
+  sp_measure_u2_body(d, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// ---------------------------------------------------------------------------
 // Launchers
 // ---------------------------------------------------------------------------
 size_t sp_cluster_smem(int V);
@@ -541,9 +704,8 @@ cudaError_t sp_launch_energy(const SpDev &d, cudaStream_t st) {
   const int G = d.NR * d.NB;
   cudaError_t e = cudaMemsetAsync(d.U2, 0, sizeof(int32_t) * (size_t)d.nw * 64 * G, st);
   if (e != cudaSuccess) return e;
-  const int chunk = sp_energy_chunk(d);
-  const long long n = (long long)d.nw * ((d.V + chunk - 1) / chunk) * G;
-  k_sp_energy<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d, chunk);
+  const long long n = (long long)d.nw * ((d.V + d.echunk - 1) / d.echunk) * G;
+  k_sp_energy<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d);
   return cudaGetLastError();
 }
 
@@ -558,22 +720,16 @@ cudaError_t sp_launch_permute(const SpDev &d, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-cudaError_t sp_launch_measure(const SpDev &d, cudaStream_t st) {
-  const long long n = (long long)d.nw * 64 * d.NR * d.NB;
-  k_sp_measure<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d);
-  return cudaGetLastError();
-}
 
 size_t sp_cluster_smem(int V) { return V <= kSpClusterMaxV ? (size_t)V * 7 : 0; }
 
 cudaError_t sp_launch_houdayer(const SpDev &d, cudaStream_t st) {
   k_sp_pairs<<<1, 32, 0, st>>>(d);
   const int ng = d.NR >= 4 ? 2 : 1;
-  const unsigned long long key = d.pt_seed ^ 0xC2B2AE3585EBCA6BULL;
   for (int g = 0; g < ng; ++g) {
     const long long n = (long long)d.nw * d.nclust * d.V;
     k_sp_overlap<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d, g);
-    k_sp_cluster<<<(unsigned)(d.nw * d.nclust * 8), 1024, sp_cluster_smem(d.V), st>>>(d, g, key);
+    k_sp_cluster<<<(unsigned)(d.nw * d.nclust * 8), 1024, sp_cluster_smem(d.V), st>>>(d, g);
     k_sp_flip<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d, g);
   }
   return cudaGetLastError();
@@ -639,6 +795,7 @@ struct ea_sp {
   ea_cadence it_cad{};
   int q_cap = 0;  // slots the overlap buffer holds
   SpDev it_dev{};  // the descriptor the graph was captured with
+  int last_itmax = 0;  // iterations of the last bin (alone or batched)
 };
 
 namespace {
@@ -693,6 +850,8 @@ int ea_sp_create(const ea_sp_geom *gp, int32_t device, ea_sp **out) {
   int maxc = 0;
   for (int k = 0; k < g.ncol; ++k) maxc = std::max(maxc, g.col_off[k + 1] - g.col_off[k]);
   d.kt = sp_kt(d.NB, d.NR, maxc);
+  d.echunk = sp_energy_chunk(d);
+  for (int k = 0; k <= g.ncol && k < 9; ++k) d.col_off[k] = g.col_off[k];
   if (!d.kt) { delete c; return spfail(EA_ERR_ARG, "NB=%d x NR=%d does not fit in shared memory", d.NB, d.NR); }
   c->device = device;
   cudaError_t e = cudaSetDevice(device);
@@ -1030,11 +1189,239 @@ int ea_sp_run(ea_sp *c, const ea_cadence *cad, double *avgE) {
     }
     for (int it = 0; it < cad->itmax; ++it) SCU(cudaGraphLaunch(c->it_graph, c->st));
   }
-  if (avgE) {
-    std::vector<double> h(n);
-    SCU(cudaMemcpyAsync(h.data(), d.avgE, n * 8, cudaMemcpyDeviceToHost, c->st));
-    SCU(cudaStreamSynchronize(c->st));
-    for (size_t i = 0; i < n; ++i) avgE[i] = h[i] / cad->itmax;
+  c->last_itmax = cad->itmax;
+  if (avgE) return ea_sp_bin_results(c, avgE);
+  return EA_OK;
+}
+
+int ea_sp_bin_results(ea_sp *c, double *avgE) {
+  if (!c || !avgE) return spfail(EA_ERR_ARG, "null argument");
+  if (c->last_itmax < 1) return spfail(EA_ERR_STATE, "no bin has run");
+  SCU(cudaSetDevice(c->device));
+  const SpDev &d = c->d;
+  const size_t n = (size_t)d.nw * 64 * d.NR * d.NB;
+  std::vector<double> h(n);
+  SCU(cudaMemcpyAsync(h.data(), d.avgE, n * 8, cudaMemcpyDeviceToHost, c->st));
+  SCU(cudaStreamSynchronize(c->st));
+  for (size_t i = 0; i < n; ++i) avgE[i] = h[i] / c->last_itmax;
+  return EA_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batches of sample-packed jobs
+// ---------------------------------------------------------------------------
+// A batch is split into classes of jobs with the same number of temperatures
+// and lattices of similar size, so that every launch is sized for its class
+// (SMEM of the thresholds and of the cluster labelling, labelling block
+// size); each class's bin iteration is a branch of one CUDA graph, so the
+// classes run side by side.
+struct SpClass {
+  std::vector<ea_sp *> jobs;
+  int ncol_max = 0, cl_threads = 1024;
+  SpDev *d_jobs = nullptr;
+  uint32_t *d_pre = nullptr;
+  std::vector<SpDev> up_jobs;
+  std::vector<uint32_t> up_pre;
+  SpBatchDev bd{};
+  cudaStream_t fs = nullptr;   // branch stream of the capture
+  cudaEvent_t join = nullptr;
+};
+
+struct ea_sp_batch {
+  std::vector<SpClass> classes;
+  std::vector<ea_sp *> jobs;
+  int device = 0;
+  cudaStream_t bs = nullptr;
+  cudaEvent_t done = nullptr, fork = nullptr;
+  cudaGraphExec_t it_graph = nullptr;
+  ea_cadence it_cad{};
+  std::vector<SpBatchDev> it_bd;
+};
+
+static int sp_size_bucket(int V) { return V <= 2048 ? 0 : V <= 8192 ? 1 : V <= kSpClusterMaxV ? 2 : 3; }
+
+static int spb_upload(SpClass &k, bool cluster, cudaStream_t bs) {
+  const int n = (int)k.jobs.size();
+  std::vector<SpDev> hj(n);
+  std::vector<uint32_t> hp((size_t)SPB_COUNT * (n + 1), 0);
+  int pass_smem = 0, perm_smem = 0, cl_smem = 0;
+  for (int i = 0; i < n; ++i) {
+    hj[i] = k.jobs[i]->d;
+    uint32_t cnt[SPB_COUNT];
+    sp_batch_blocks(hj[i], cluster, cnt);
+    for (int q = 0; q < SPB_COUNT; ++q) hp[(size_t)q * (n + 1) + i + 1] = hp[(size_t)q * (n + 1) + i] + cnt[q];
+    pass_smem = std::max(pass_smem, (int)sp_sweep_smem(hj[i].NB, hj[i].NR, hj[i].kt));
+    perm_smem = std::max(perm_smem, kPermRows * hj[i].NB * 8);
+    if (cluster) cl_smem = std::max(cl_smem, (int)sp_cluster_smem(hj[i].V));
+  }
+  if (k.up_jobs.size() != hj.size() || std::memcmp(k.up_jobs.data(), hj.data(), sizeof(SpDev) * n) ||
+      k.up_pre != hp) {
+    SCU(cudaStreamSynchronize(bs));
+    SCU(cudaMemcpy(k.d_jobs, hj.data(), sizeof(SpDev) * n, cudaMemcpyHostToDevice));
+    SCU(cudaMemcpy(k.d_pre, hp.data(), sizeof(uint32_t) * hp.size(), cudaMemcpyHostToDevice));
+    k.up_jobs = hj;
+    k.up_pre = hp;
+  }
+  SpBatchDev &bd = k.bd;
+  bd = SpBatchDev{};
+  bd.jobs = k.d_jobs;
+  bd.njobs = n;
+  for (int q = 0; q < SPB_COUNT; ++q) {
+    bd.pre[q] = k.d_pre + (size_t)q * (n + 1);
+    bd.total[q] = hp[(size_t)q * (n + 1) + n];
+  }
+  bd.pass_smem = pass_smem;
+  bd.perm_smem = perm_smem;
+  bd.cluster_smem = cl_smem;
+  bd.cluster_threads = k.cl_threads;
+  return EA_OK;
+}
+
+static cudaError_t spb_iteration(const SpClass &k, const ea_cadence *cad, cudaStream_t st) {
+  cudaError_t e = cudaSuccess;
+  for (int im = 0; im < cad->mesfr && e == cudaSuccess; ++im) {
+    for (int ih = 0; ih < cad->houfr && e == cudaSuccess; ++ih) {
+      for (int sw = 0; sw < cad->ptfr && e == cudaSuccess; ++sw) e = sp_batch_sweep(k.bd, k.ncol_max, st);
+      if (e == cudaSuccess) e = sp_batch_tempering(k.bd, st);
+    }
+    if (e == cudaSuccess && cad->cluster) e = sp_batch_houdayer(k.bd, st);
+  }
+  if (e == cudaSuccess) e = sp_batch_measure(k.bd, st);
+  return e;
+}
+
+extern "C" {
+
+int ea_sp_batch_create(ea_sp *const *jobs, int32_t njobs, ea_sp_batch **out) {
+  if (!jobs || !out || njobs < 1) return spfail(EA_ERR_ARG, "at least one job");
+  ea_sp_batch *b = new ea_sp_batch();
+  std::vector<std::pair<int, int>> keys;
+  for (int i = 0; i < njobs; ++i) {
+    ea_sp *c = jobs[i];
+    if (!c || std::find(b->jobs.begin(), b->jobs.end(), c) != b->jobs.end()) {
+      delete b;
+      return spfail(EA_ERR_ARG, "job %d is null or appears twice", i);
+    }
+    if (i && c->device != b->device) { delete b; return spfail(EA_ERR_ARG, "the jobs of a batch share the device"); }
+    if (c->d.ncol > kSpBatchMaxColours) {
+      delete b;
+      return spfail(EA_ERR_ARG, "job %d needs %d colours (a batch takes %d)", i, c->d.ncol, kSpBatchMaxColours);
+    }
+    b->device = c->device;
+    b->jobs.push_back(c);
+    const std::pair<int, int> key(c->d.NB, sp_size_bucket(c->d.V));
+    size_t q = std::find(keys.begin(), keys.end(), key) - keys.begin();
+    if (q == keys.size()) {
+      keys.push_back(key);
+      b->classes.emplace_back();
+      b->classes.back().cl_threads = key.second == 0 ? 256 : key.second == 1 ? 512 : 1024;
+    }
+    SpClass &k = b->classes[q];
+    k.jobs.push_back(c);
+    k.ncol_max = std::max(k.ncol_max, c->d.ncol);
+  }
+  cudaError_t e = cudaSetDevice(b->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->bs, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+  for (SpClass &k : b->classes) {
+    const size_t n = k.jobs.size();
+    if (e == cudaSuccess) e = cudaMalloc((void **)&k.d_jobs, sizeof(SpDev) * n);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&k.d_pre, sizeof(uint32_t) * SPB_COUNT * (n + 1));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&k.fs, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&k.join, cudaEventDisableTiming);
+  }
+  if (e == cudaSuccess) e = sp_batch_setup();
+  if (e != cudaSuccess) {
+    ea_sp_batch_destroy(b);
+    return spfail(EA_ERR_CUDA, "batch set-up: %s", cudaGetErrorString(e));
+  }
+  *out = b;
+  return EA_OK;
+}
+
+int ea_sp_batch_destroy(ea_sp_batch *b) {
+  if (!b) return EA_OK;
+  cudaSetDevice(b->device);
+  if (b->bs) cudaStreamSynchronize(b->bs);
+  if (b->it_graph) cudaGraphExecDestroy(b->it_graph);
+  for (SpClass &k : b->classes) {
+    if (k.d_jobs) cudaFree(k.d_jobs);
+    if (k.d_pre) cudaFree(k.d_pre);
+    if (k.join) cudaEventDestroy(k.join);
+    if (k.fs) cudaStreamDestroy(k.fs);
+  }
+  if (b->done) cudaEventDestroy(b->done);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->bs) cudaStreamDestroy(b->bs);
+  delete b;
+  return EA_OK;
+}
+
+int ea_sp_batch_stream(ea_sp_batch *b, void **stream) {
+  if (!b || !stream) return spfail(EA_ERR_ARG, "null argument");
+  *stream = (void *)b->bs;
+  return EA_OK;
+}
+
+int ea_sp_batch_sync(ea_sp_batch *b) {
+  if (!b) return spfail(EA_ERR_ARG, "null batch");
+  SCU(cudaSetDevice(b->device));
+  SCU(cudaStreamSynchronize(b->bs));
+  return EA_OK;
+}
+
+int ea_sp_batch_run(ea_sp_batch *b, const ea_cadence *cad) {
+  if (!b || !cad || cad->itmax < 1 || cad->houfr < 1 || cad->mesfr < 1 || cad->ptfr < 1)
+    return spfail(EA_ERR_ARG, "bad cadence");
+  SCU(cudaSetDevice(b->device));
+  int rc;
+  for (ea_sp *c : b->jobs) {
+    if (!c->have_temps) return spfail(EA_ERR_STATE, "temperatures not set");
+    int nclust = cad->nclust;
+    if (cad->cluster && (rc = sp_cluster_prepare(c, nclust))) return rc;
+    // every job's earlier work comes first
+    SCU(cudaEventRecord(b->done, c->st));
+    SCU(cudaStreamWaitEvent(b->bs, b->done, 0));
+  }
+  std::vector<SpBatchDev> bds;
+  for (SpClass &k : b->classes) {
+    if ((rc = spb_upload(k, cad->cluster != 0, b->bs))) return rc;
+    bds.push_back(k.bd);
+  }
+  for (ea_sp *c : b->jobs)
+    SCU(cudaMemsetAsync(c->d.avgE, 0, sizeof(double) * (size_t)c->d.nw * 64 * c->d.NR * c->d.NB, b->bs));
+  if (!b->it_graph || std::memcmp(&b->it_cad, cad, sizeof(ea_cadence)) || b->it_bd.size() != bds.size() ||
+      std::memcmp(b->it_bd.data(), bds.data(), sizeof(SpBatchDev) * bds.size())) {
+    if (b->it_graph) { cudaGraphExecDestroy(b->it_graph); b->it_graph = nullptr; }
+    cudaGraph_t graph = nullptr;
+    SCU(cudaStreamBeginCapture(b->bs, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaEventRecord(b->fork, b->bs);
+    for (SpClass &k : b->classes) {
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(k.fs, b->fork, 0);
+      if (e == cudaSuccess) e = spb_iteration(k, cad, k.fs);
+      if (e == cudaSuccess) e = cudaEventRecord(k.join, k.fs);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(b->bs, k.join, 0);
+    }
+    const cudaError_t ec = cudaStreamEndCapture(b->bs, &graph);
+    if (e != cudaSuccess || ec != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      return spfail(EA_ERR_CUDA, "batch capture: %s", cudaGetErrorString(e != cudaSuccess ? e : ec));
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&b->it_graph, graph, 0);
+    cudaGraphDestroy(graph);
+    SCU(ei);
+    b->it_cad = *cad;
+    b->it_bd = bds;
+  }
+  for (int it = 0; it < cad->itmax; ++it) SCU(cudaGraphLaunch(b->it_graph, b->bs));
+  // later work of each job comes after the batch
+  SCU(cudaEventRecord(b->done, b->bs));
+  for (ea_sp *c : b->jobs) {
+    SCU(cudaStreamWaitEvent(c->st, b->done, 0));
+    c->last_itmax = cad->itmax;
   }
   return EA_OK;
 }

@@ -38,6 +38,8 @@ void sp_spins(const SpGraph &g, int nwords, int NR, int NB, uint64_t seed_u, uin
 // Device view of a sample-packed job (kernel parameter).
 struct SpDev {
   int L, Lz, V, bc, NB, NR, nw, ncol, kt;
+  int echunk;                        // sites per thread of the energy count
+  int col_off[9];                    // colour c owns col_sites[col_off[c] .. col_off[c+1])
   const int32_t *nb;                 // [V][6]
   const int32_t *col_sites;          // [V]
   unsigned long long *S;             // [nw][V][NR][NB] spin words
@@ -79,16 +81,40 @@ constexpr int kSpClusterMaxV = 32768;
 __host__ __device__ inline size_t sp_cluster_words(int V) { return ((size_t)V * 7 + 15) / 16 * 4; }
 
 int sp_kt(int NB, int NR, int nsites_colour);
+int sp_energy_chunk(const SpDev &d);
 size_t sp_sweep_smem(int NB, int NR, int kt);
 cudaError_t sp_setup();
 cudaError_t sp_launch_pass(const SpDev &d, int colour, int off, int n, cudaStream_t st);
 cudaError_t sp_launch_energy(const SpDev &d, cudaStream_t st);
 cudaError_t sp_launch_pt(const SpDev &d, cudaStream_t st);
 cudaError_t sp_launch_permute(const SpDev &d, cudaStream_t st);
-cudaError_t sp_launch_measure(const SpDev &d, cudaStream_t st);
 cudaError_t sp_launch_houdayer(const SpDev &d, cudaStream_t st);
 cudaError_t sp_launch_measure_u2(const SpDev &d, cudaStream_t st);
 cudaError_t sp_launch_dos(const SpDev &d, cudaStream_t st);
 cudaError_t sp_launch_exact(const SpDev &d, const double *betas, int nbeta, double *meanE, cudaStream_t st);
+
+// Batched sample-packed kernels: one launch per kernel kind for every job of
+// a batch, block b of a launch working for the job j with pre[j] <= b < pre[j+1].
+enum {
+  SPB_PASS0 = 0, SPB_PASS1, SPB_PASS2, SPB_PASS3,  // colour passes (jobs with that colour)
+  SPB_ZERO, SPB_ENERGY, SPB_PT, SPB_PERMUTE, SPB_MEASURE,
+  SPB_OVL0, SPB_OVL1, SPB_CL0, SPB_CL1, SPB_FL0, SPB_FL1,  // Houdayer, per replica group
+  SPB_COUNT
+};
+constexpr int kSpBatchMaxColours = 4;
+struct SpBatchDev {
+  const SpDev *jobs;
+  int njobs;
+  const uint32_t *pre[SPB_COUNT];
+  uint32_t total[SPB_COUNT];
+  int pass_smem, perm_smem, cluster_smem;  // dynamic SMEM of the largest job
+  int cluster_threads;                      // block size of the labelling
+};
+void sp_batch_blocks(const SpDev &d, bool cluster, uint32_t out[SPB_COUNT]);
+cudaError_t sp_batch_setup();
+cudaError_t sp_batch_sweep(const SpBatchDev &b, int ncol_max, cudaStream_t st);
+cudaError_t sp_batch_tempering(const SpBatchDev &b, cudaStream_t st);
+cudaError_t sp_batch_houdayer(const SpBatchDev &b, cudaStream_t st);
+cudaError_t sp_batch_measure(const SpBatchDev &b, cudaStream_t st);
 
 }  // namespace eagb

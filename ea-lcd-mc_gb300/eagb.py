@@ -553,6 +553,11 @@ class SpJob:
         cad = Cadence(itmax, houfr, mesfr, ptfr, int(cluster), nclust)
         _ck(lib().ea_sp_run(self.h, C.byref(cad), None))
 
+    def bin_results(self):
+        avg = np.zeros((self.g.nwords, 64, self.g.nrep, self.g.nbetas))
+        _ck(lib().ea_sp_bin_results(self.h, P(avg)))
+        return avg
+
     def exact(self, betas=None):
         """Density of states [nwords*64, 6V+1] and <E>(beta) [nwords*64, NB] (V <= 32)."""
         b = np.ascontiguousarray(self.betas if betas is None else betas, np.float64)
@@ -574,3 +579,30 @@ class SpView(SpJob):
 
     def close(self):
         self.h = None
+
+
+class SpBatch:
+    """Sample-packed jobs advanced together by the batched kernels (ea_sp_batch)."""
+
+    def __init__(self, jobs):
+        self.jobs = list(jobs)
+        arr = (C.c_void_p * len(self.jobs))(*[j.h.value if isinstance(j.h, C.c_void_p) else j.h for j in self.jobs])
+        self.b = C.c_void_p()
+        _ck(lib().ea_sp_batch_create(arr, len(self.jobs), C.byref(self.b)))
+
+    def run_bin(self, itmax, houfr=1, mesfr=1, ptfr=1, cluster=False, nclust=0):
+        cad = Cadence(itmax, houfr, mesfr, ptfr, int(cluster), nclust)
+        _ck(lib().ea_sp_batch_run(self.b, C.byref(cad)))
+
+    def sync(self):
+        _ck(lib().ea_sp_batch_sync(self.b))
+
+    def stream(self):
+        v = C.c_void_p()
+        _ck(lib().ea_sp_batch_stream(self.b, C.byref(v)))
+        return v.value
+
+    def close(self):
+        if self.b:
+            _ck(lib().ea_sp_batch_destroy(self.b))
+            self.b = None

@@ -332,6 +332,22 @@ int ea_sp_houdayer(ea_sp *job, int32_t nclust);
  * measurement]; avgE [nwords][64][NR][NB] (may be NULL) = the bin's average
  * energy of each slot. */
 int ea_sp_run(ea_sp *job, const ea_cadence *cad, double *avgE);
+/* The last bin's average energies (by ea_sp_run or a batch), as ea_sp_run returns them. */
+int ea_sp_bin_results(ea_sp *job, double *avgE);
+/* Batches of sample-packed jobs (any geometries, replica and temperature
+ * counts, up to 4 colours each).  Jobs are grouped in classes of equal NB
+ * and similar lattice size; each class takes one launch per kernel kind over
+ * a packed (job, block) work list, sized for the class, and one bin
+ * iteration of all classes -- side by side, one branch each -- is replayed
+ * as a CUDA graph.  Each job's words, energies and swaps equal those of
+ * ea_sp_run on the job alone.  Asynchronous; read results with
+ * ea_sp_bin_results. */
+typedef struct ea_sp_batch ea_sp_batch;
+int ea_sp_batch_create(ea_sp *const *jobs, int32_t njobs, ea_sp_batch **out);
+int ea_sp_batch_run(ea_sp_batch *b, const ea_cadence *cad);
+int ea_sp_batch_sync(ea_sp_batch *b);
+int ea_sp_batch_stream(ea_sp_batch *b, void **stream);
+int ea_sp_batch_destroy(ea_sp_batch *b);
 /* Exact enumeration (V <= 32): dos [nwords*64][6V+1] configurations with
  * spin 0 up at each E = -3V..3V, and meanE [nwords*64][nbeta] = <E>(beta)
  * from it in FP64 on the GPU. */

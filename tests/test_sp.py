@@ -307,3 +307,31 @@ def test_monte_carlo_matches_exact_enumeration(bc, cluster):
     assert np.abs(z).max() < 6.0, np.abs(z).max()
     assert 0.5 < (z ** 2).mean() < 2.0, (z ** 2).mean()
     job.close()
+
+
+BATCH = [(3, 3, eagb.EA_PBC, "T07_16_N8", 2, 1), (5, 7, eagb.EA_OBC, "T07_16_N6", 4, 2),
+         (8, 16, eagb.EA_OBC, "T07_16_N24", 2, 1), (6, 12, eagb.EA_PBC, "T08_16_N4", 4, 3),
+         (19, 96, eagb.EA_OBC, "T08_16_N4", 2, 1)]
+
+
+@pytest.mark.gpu
+def test_batch_equals_jobs_alone():
+    """A batch of sample-packed jobs of different L (odd and even, 2 and 3
+    colours), Lz, boundary, replica, temperature and word counts, one
+    lattice above the SMEM labelling limit: every job ends as if run alone."""
+    alone = [new_job(*c, jobid=40 + k) for k, c in enumerate(BATCH)]
+    batched = [new_job(*c, jobid=40 + k) for k, c in enumerate(BATCH)]
+    batch = eagb.SpBatch(batched)
+    for itmax, houfr, mesfr, ptfr, cl in [(2, 2, 1, 1, True), (3, 1, 2, 2, False), (1, 3, 1, 1, True)]:
+        batch.run_bin(itmax, houfr, mesfr, ptfr, cluster=cl)
+        for a, b in zip(alone, batched):
+            avg = a.run_bin(itmax, houfr, mesfr, ptfr, cluster=cl)
+            assert np.array_equal(avg, b.bin_results())
+    batch.sync()
+    for a, b in zip(alone, batched):
+        assert np.array_equal(a.get_spins(), b.get_spins())
+        assert all(np.array_equal(x, y) for x, y in zip(a.tempering(), b.tempering()))
+        assert a.counter() == b.counter()
+    batch.close()
+    for j in alone + batched:
+        j.close()
