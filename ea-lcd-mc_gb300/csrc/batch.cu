@@ -72,7 +72,8 @@ __global__ void __launch_bounds__(512) kb_sweep(const __grid_constant__ BatchDev
   int staged = -1;  // job whose thresholds are in SMEM
   BATCH_LOOP(KB_SWEEP) {
     const int jb = item_job(pre, b.njobs, v);
-    sweep_body<NR, KT, UPDATE>(b.jobs[jb], (int)(v - __ldg(pre + jb)), parity, energy, smem, jb != staged);
+    const JobDev jd = b.jobs[jb];  // a copy: no aliasing with the job's arrays
+    sweep_body<NR, KT, UPDATE>(jd, (int)(v - __ldg(pre + jb)), parity, energy, smem, jb != staged);
     staged = jb;
     __syncthreads();
   }
@@ -92,7 +93,7 @@ __global__ void __launch_bounds__(256) kb_pt(const __grid_constant__ BatchDev b)
   __shared__ uint8_t s_wc[8][256];
   BATCH_LOOP(KB_PT) {
     const int jb = item_job(pre, b.njobs, v);
-    const JobDev &j = b.jobs[jb];
+    const JobDev j = b.jobs[jb];
     const int l = (int)(v - __ldg(pre + jb));
     pt_body(j, l % j.ns, l / j.ns, s_ira, s_wc);
     __syncthreads();
@@ -116,7 +117,7 @@ __global__ void kb_pairs(const __grid_constant__ BatchDev b) {
 __global__ void kb_overlap(const __grid_constant__ BatchDev b, int g) {
   BATCH_LOOP(KB_OVERLAP) {
     const int jb = item_job(pre, b.njobs, v);
-    const JobDev &j = b.jobs[jb];
+    const JobDev j = b.jobs[jb];
     const int gx = (2 * j.half + 255) / 256, l = (int)(v - __ldg(pre + jb));
     overlap_body(j, g, (l % gx) * 256 + threadIdx.x, (size_t)(l / gx));
   }
@@ -128,7 +129,7 @@ __global__ void __launch_bounds__(1024, 2) kb_cc_slab(const __grid_constant__ Ba
   __shared__ uint8_t qs[kSlabSites];
   BATCH_LOOP(KB_SLAB) {
     const int jb = item_job(pre, b.njobs, v);
-    const JobDev &j = b.jobs[jb];
+    const JobDev j = b.jobs[jb];
     int D, P, nslab;
     dev_slab_shape(j, D, P, nslab);
     const int l = (int)(v - __ldg(pre + jb));
@@ -141,7 +142,7 @@ __global__ void __launch_bounds__(1024, 2) kb_cc_slab(const __grid_constant__ Ba
 __global__ void kb_cc_merge(const __grid_constant__ BatchDev b) {
   BATCH_LOOP(KB_MERGE) {
     const int jb = item_job(pre, b.njobs, v);
-    const JobDev &j = b.jobs[jb];
+    const JobDev j = b.jobs[jb];
     int D, P, nslab;
     dev_slab_shape(j, D, P, nslab);
     const int gx = (nslab * j.L * j.L + 255) / 256, l = (int)(v - __ldg(pre + jb));
@@ -153,7 +154,7 @@ __global__ void kb_cc_merge(const __grid_constant__ BatchDev b) {
 __global__ void kb_cc_compress(const __grid_constant__ BatchDev b) {
   BATCH_LOOP(KB_COMPRESS) {
     const int jb = item_job(pre, b.njobs, v);
-    const JobDev &j = b.jobs[jb];
+    const JobDev j = b.jobs[jb];
     int D, P, nslab;
     dev_slab_shape(j, D, P, nslab);
     const int gx = (nslab * j.L * j.L + 255) / 256, l = (int)(v - __ldg(pre + jb));
@@ -167,7 +168,8 @@ __global__ void __launch_bounds__(512) kb_flip(const __grid_constant__ BatchDev 
   extern __shared__ uint32_t s_flip[];
   BATCH_LOOP(KB_FLIP) {
     const int jb = item_job(pre, b.njobs, v);
-    flip_body(b.jobs[jb], u.u[jb], g, (size_t)(v - __ldg(pre + jb)), s_flip + 64, reinterpret_cast<int *>(s_flip));
+    const JobDev jd = b.jobs[jb];
+    flip_body(jd, u.u[jb], g, (size_t)(v - __ldg(pre + jb)), s_flip + 64, reinterpret_cast<int *>(s_flip));
     __syncthreads();
   }
   }

@@ -335,11 +335,11 @@ int ea_sp_run(ea_sp *job, const ea_cadence *cad, double *avgE);
 /* The last bin's average energies (by ea_sp_run or a batch), as ea_sp_run returns them. */
 int ea_sp_bin_results(ea_sp *job, double *avgE);
 /* Batches of sample-packed jobs (any geometries, replica and temperature
- * counts, up to 4 colours each).  Jobs are grouped in classes of equal NB
- * and similar lattice size; each class takes one launch per kernel kind over
- * a packed (job, block) work list, sized for the class, and one bin
- * iteration of all classes -- side by side, one branch each -- is replayed
- * as a CUDA graph.  Each job's words, energies and swaps equal those of
+ * counts, up to 4 colours each).  Jobs are grouped in classes (one per job
+ * for up to 256 jobs, else of equal NB and similar lattice size); each class
+ * takes one launch per kernel kind over a packed (job, block) work list,
+ * sized for the class, and one bin iteration of all classes -- side by side,
+ * one graph branch each -- is replayed as one CUDA graph launch.  Each job's words, energies and swaps equal those of
  * ea_sp_run on the job alone.  Asynchronous; read results with
  * ea_sp_bin_results. */
 typedef struct ea_sp_batch ea_sp_batch;
