@@ -335,3 +335,27 @@ def test_batch_equals_jobs_alone():
     batch.close()
     for j in alone + batched:
         j.close()
+
+
+@pytest.mark.gpu
+def test_large_batch_classes_equal_jobs_alone():
+    """Above 256 jobs a batch groups jobs into classes of equal NB and lattice
+    size (one launch per kernel kind for a whole class): 260 small jobs of
+    five geometries still end as if run alone."""
+    geoms = [(2, 2, eagb.EA_PBC, "T08_16_N4", 2, 1), (3, 3, eagb.EA_OBC, "T07_16_N6", 4, 1),
+             (2, 4, eagb.EA_OBC, "T07_16_N6", 2, 1), (4, 2, eagb.EA_PBC, "T08_16_N4", 4, 1),
+             (3, 5, eagb.EA_PBC, "T07_16_N8", 2, 1)]
+    cases = [geoms[k % len(geoms)] for k in range(260)]
+    alone = [new_job(*c, jobid=k) for k, c in enumerate(cases)]
+    batched = [new_job(*c, jobid=k) for k, c in enumerate(cases)]
+    batch = eagb.SpBatch(batched)
+    batch.run_bin(2, 2, 1, 1, cluster=True)
+    for a in alone:
+        a.run_bin(2, 2, 1, 1, cluster=True)
+    batch.sync()
+    for a, b in zip(alone, batched):
+        assert np.array_equal(a.get_spins(), b.get_spins())
+        assert np.array_equal(a.bin_results(), b.bin_results())
+    batch.close()
+    for j in alone + batched:
+        j.close()
