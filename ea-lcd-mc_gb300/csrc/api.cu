@@ -529,6 +529,15 @@ int ea_set_spins(ea_ctx *c, int32_t s, const uint64_t *even, const uint64_t *odd
   return EA_OK;
 }
 
+int ea_upload_spins_async(ea_ctx *c, const uint64_t *all) {
+  if (check(c) || !all) return fail(EA_ERR_ARG, "bad arguments");
+  if (set_device(c)) return EA_ERR_CUDA;
+  const size_t n = (size_t)c->g.ns * c->g.words_per_sample();
+  CU(cudaMemcpyAsync(c->j.spins, all, n * 8, cudaMemcpyHostToDevice, c->st));
+  c->energies_fresh = false;
+  return EA_OK;
+}
+
 int ea_get_spins(ea_ctx *c, int32_t s, uint64_t *even, uint64_t *odd) {
   if (check(c) || s < 0 || s >= c->g.ns || !even || !odd) return fail(EA_ERR_ARG, "bad arguments");
   const size_t n = c->g.words_per_parity();

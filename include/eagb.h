@@ -134,6 +134,13 @@ int ea_join(ea_ctx *ctx);
 int ea_set_temperatures(ea_ctx *ctx, const double *betas, const uint64_t *cum);
 int ea_set_spins(ea_ctx *ctx, int32_t sample, const uint64_t *even, const uint64_t *odd);
 int ea_get_spins(ea_ctx *ctx, int32_t sample, uint64_t *even, uint64_t *odd);
+/* The spins of every sample, [nsamples][2][NB][half][NR] (each sample's even
+ * then odd array, as ea_set_spins takes them), in one copy enqueued on the
+ * context's stream without a host synchronisation: the buffer should be
+ * pinned (cudaHostAlloc) and stay unchanged until the stream has passed the
+ * copy (ea_sync, or a later call that returns data).  No reference
+ * counterpart (the reference uploads at start-up and restarts only). */
+int ea_upload_spins_async(ea_ctx *ctx, const uint64_t *all);
 int ea_set_couplings(ea_ctx *ctx, int32_t sample, const uint64_t *Jw);
 /* pt: [nsamples][NR] PT generators (random_PT, header.h:133). */
 int ea_set_generators(ea_ctx *ctx, const ea_generators *gen, const ea_hq *pt);

@@ -114,3 +114,21 @@ def test_batch_matches_oracle():
     batch.close()
     for j in jobs:
         j.close()
+
+
+def test_upload_spins_async():
+    """ea_upload_spins_async: one copy of every sample's spins, read back as
+    ea_get_spins returns them."""
+    import ctypes as C
+    L, Lz, ln, bc, ns = MIX[3]
+    betas, cum = lut(ln)
+    job = eagb.new_job(L, Lz, betas, cum, nsamples=ns, bc=bc, masters=MASTERS, iter0=0, jobid=3)
+    rng = np.random.default_rng(5)
+    nw = len(job.get_spins(0)[0])
+    allw = rng.integers(0, 2 ** 63, size=(ns, 2, nw), dtype=np.int64).view(np.uint64)
+    eagb._ck(eagb.lib().ea_upload_spins_async(job.ctx, eagb.P(allw)))
+    job.sync()
+    for s in range(ns):
+        ev, od = job.get_spins(s)
+        assert np.array_equal(ev, allw[s, 0]) and np.array_equal(od, allw[s, 1])
+    job.close()
