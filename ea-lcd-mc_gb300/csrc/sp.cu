@@ -125,11 +125,13 @@ constexpr int kSpChunkMax = 256;  // sites per thread: 6 * 256 < 2^11
 constexpr int kSpPlanes = 11;
 
 // Sites per thread of the energy kernel: enough threads to fill the GPU
-// (152 SMs x 2048), at least 8 sites each.
+// (152 SMs x 2048), at least 16 sites each (each thread ends with 64 atomic
+// additions, which small chunks pile on the same counters; larger chunks
+// leave small jobs with too few threads -- 8 and 32 measured either side).
 int sp_energy_chunk(const SpDev &d) {
   const double words = (double)d.nw * d.V * d.NR * d.NB;
   int c = (int)(words / (152.0 * 2048.0));
-  return c < 8 ? 8 : (c > kSpChunkMax ? kSpChunkMax : c);
+  return c < 16 ? 16 : (c > kSpChunkMax ? kSpChunkMax : c);
 }
 
 __device__ __forceinline__ void sp_energy_body(const SpDev &d, int blk) {
@@ -668,16 +670,18 @@ size_t sp_sweep_smem(int NB, int NR, int kt) {
   return (size_t)NB * 256 * 10 + (size_t)3 * NB * kt * NR * 8 + (size_t)kt * 7 * 4;
 }
 
-// Tile width: the widest power of two up to 64 whose SMEM fits and that still
-// gives two tiles per SM, else the widest that fits.
+// Tile width: the smallest power of two whose random triples (NB x kt x NR)
+// fill half of the CTA's 512 threads -- narrower tiles leave the CTA staging
+// every threshold table for a few words -- then doubled while two tiles per
+// SM remain and SMEM fits (large jobs amortise the staging over more sites).
 int sp_kt(int NB, int NR, int nsites_colour) {
-  int best = 0;
-  for (int kt = 64; kt >= 1; kt >>= 1) {
-    if (sp_sweep_smem(NB, NR, kt) > 227 * 1024) continue;
-    if (!best) best = kt;
-    if ((nsites_colour + kt - 1) / kt >= 2 * 152) return kt;
-  }
-  return best;
+  int kt = 1;
+  while (kt < 64 && NB * kt * NR < 256) kt <<= 1;
+  while (kt > 1 && sp_sweep_smem(NB, NR, kt) > 227 * 1024) kt >>= 1;
+  if (sp_sweep_smem(NB, NR, kt) > 227 * 1024) return 0;
+  while (kt < 64 && sp_sweep_smem(NB, NR, 2 * kt) <= 227 * 1024 && (nsites_colour + 2 * kt - 1) / (2 * kt) >= 2 * 152)
+    kt <<= 1;
+  return kt;
 }
 
 cudaError_t sp_setup() {
