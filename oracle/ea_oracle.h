@@ -114,7 +114,7 @@ void or_cluster_roots(const or_geom *g, const uint8_t *q /*[V]*/, uint32_t *root
 
 /* ---- LUT (create_LUT.c) ----------------------------------------------------- */
 /* Cumulative thresholds and the reference file layout of one beta.  Returns 0 on
- * success, -1 if quad precision is not available in this build. */
+ * success, -1 when the oracle was compiled without quad precision. */
 int or_lut_beta(double beta, int nbits_pre, uint64_t *cum /*[256]*/, uint32_t *umbrales /*[512]*/,
                 uint32_t *prebusqueda /*[(1<<nbits_pre)/2]*/);
 

@@ -13,11 +13,12 @@ Step 2 (on the GPU host, from the repository root):
     bash oracle/_ref/runs/run_all.sh
   builds one reference executable per case with plain nvcc/g++ lines
   (oracle/Makefile, target ref-cuda; not the reference's own Makefile), runs
-  it, and copies each output tree to gpurun_out/refgold/<tag>/.
+  it, and copies each output tree to <OUT>/<tag>/, OUT being the folder that
+  the GPU host hands back (EA_REFGOLD_OUT, relative to the repository root).
 
 Step 3 (here):
     python tests/golden/make_ref_golden.py collect
-  turns gpurun_out/refgold/ into tests/golden/ref_<tag>.npz: every output file
+  turns <OUT>/ into tests/golden/ref_<tag>.npz: every output file
   of every (sample, replica) -- whole when small, SHA-256 otherwise.
 """
 import hashlib
@@ -33,6 +34,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 ORACLE = os.path.join(ROOT, "oracle")
 RUNS = os.path.join(ORACLE, "_ref", "runs")
 REF = os.environ.get("EA_REF", "/root/reference/PROGRAM")
+OUT = os.environ.get("EA_REFGOLD_OUT", os.path.join("gpurun_out", "refgold"))
 MASTERS = (81985529216486895, 1147797409030816545, 1229782938247303441, 6148914691236517205)
 
 # tag: L, Lz, BC, cluster, lut-set, isample, nbits, list_samples, nbin, itmax, houfr, mesfr, ptfr, resume_nbin
@@ -70,14 +72,14 @@ def stage():
     shutil.rmtree(RUNS, ignore_errors=True)
     subprocess.run(["make", "-s", "-C", ORACLE, "ref-stage"], check=True)
     lines = ["#!/bin/bash", "# builds and runs the reference binary for every golden case (GPU host)",
-             "set -u", "cd \"$(dirname \"$0\")/../../..\"", "R=$PWD", "mkdir -p gpurun_out/refgold",
-             "nvidia-smi -L > gpurun_out/refgold/gpu.txt 2>&1", "builds=()"]
+             "set -u", "cd \"$(dirname \"$0\")/../../..\"", "R=$PWD", "mkdir -p %s" % OUT,
+             "nvidia-smi -L > %s/gpu.txt 2>&1" % OUT, "builds=()"]
     runs = []
     for tag, (L, Lz, BC, cl, lutname, isample, nbits, lst, nbin, itmax, houfr, mesfr, ptfr, resume) in CASES.items():
         nb = case_inputs(tag, os.path.join(RUNS, tag))
         cfg = "%d,%d,%d,%s" % (L, Lz, nb, BC)
         exe = "oracle/_ref/bin/EA_L%d_Lz%d_NB%d_%s%s" % (L, Lz, nb, BC, "" if cl else "_NOCL")
-        lines.append("make -s -C oracle ref-cuda CFG=%s CLUSTER=%d > gpurun_out/refgold/build_%s.log 2>&1 &" % (cfg, cl, tag))
+        lines.append("make -s -C oracle ref-cuda CFG=%s CLUSTER=%d > %s/build_%s.log 2>&1 &" % (cfg, cl, OUT, tag))
         args = "%d %d betas input.in LUT 0 0%s" % (isample, nbits, " list" if lst else "")
         runs.append((tag, exe, args, resume))
     for tag, (nbits, nbin, itmax, houfr) in TIMING.items():
@@ -88,14 +90,14 @@ def stage():
         lines.append("( cd oracle/_ref/runs/%s && \"$R/%s\" %s > run.log 2>&1 ; echo rc=$? >> run.log )" % (tag, exe, args))
         if resume:
             lines.append("( cd oracle/_ref/runs/%s && sed -i '2s/.*/%d/;9s/.*/0/' input.in && \"$R/%s\" %s > resume.log 2>&1 ; echo rc=$? >> resume.log )" % (tag, resume, exe, args))
-        lines.append("mkdir -p gpurun_out/refgold/%s && cp -r oracle/_ref/runs/%s/. gpurun_out/refgold/%s/ && rm -f gpurun_out/refgold/%s/LUT" % (tag, tag, tag, tag))
+        lines.append("mkdir -p %s/%s && cp -r oracle/_ref/runs/%s/. %s/%s/ && rm -f %s/%s/LUT" % (OUT, tag, tag, OUT, tag, OUT, tag))
     with open(os.path.join(RUNS, "run_all.sh"), "w") as f:
         f.write("\n".join(lines) + "\n")
     print("staged", len(runs), "cases in", RUNS)
 
 
 def collect():
-    src = os.path.join(ROOT, "gpurun_out", "refgold")
+    src = os.path.join(ROOT, OUT)
     for tag in CASES:
         base = os.path.join(src, tag)
         if not os.path.isdir(base):
