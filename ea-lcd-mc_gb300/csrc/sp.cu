@@ -398,6 +398,107 @@ __device__ __forceinline__ void sp_cluster_body(const SpDev &d, int g, int blk, 
   for (int i = threadIdx.x; i < V; i += blockDim.x) Qb[(size_t)i * 8] = fb[i];
 }
 
+// The same labelling for 4 samples at a time, for lattices up to
+// kSpCluster4MaxV sites: a site's 4 labels sit in one 16-byte SMEM slot and
+// its 4 bond masks in one word (sample l at bits 8l..8l+5), so that one
+// neighbour-table load and one loop step serve the 4 samples (the 1-sample
+// form spends ~600 instructions per site and lattice, mostly on those).
+// Roots, coins and flip bytes are those of sp_cluster_body.
+__device__ __forceinline__ uint32_t spread4(uint32_t x) {
+  return (x & 1u) | ((x & 2u) << 7) | ((x & 4u) << 14) | ((x & 8u) << 21);
+}
+
+__device__ __forceinline__ void sp_cluster4_body(const SpDev &d, int g, int blk, uint32_t *sm) {
+  const unsigned long long key = sp_cluster_key(d);
+  const int V = d.V, nc = d.nclust;
+  uint4 *lab = reinterpret_cast<uint4 *>(sm);                          // [V]
+  uint32_t *lab1 = sm;                                                 // the same, one label per word
+  uint32_t *bond = sm + 4 * (size_t)V;                                 // [V]
+  uint8_t *qb = reinterpret_cast<uint8_t *>(bond + V);                 // [V]
+  uint8_t *fb = qb + V;                                                // [V]
+  const int grp = blk & 7, lat = blk >> 3;
+  const int b = lat % nc, w = lat / nc;
+  uint8_t *Qb = reinterpret_cast<uint8_t *>(d.Q + (size_t)lat * V) + grp;
+  for (int i = threadIdx.x; i < V; i += blockDim.x) {
+    qb[i] = Qb[(size_t)i * 8];
+    fb[i] = 0;
+  }
+  __syncthreads();
+  const unsigned long long mv = *d.move;
+  for (int h = 0; h < 2; ++h) {
+    for (int i = threadIdx.x; i < V; i += blockDim.x) {
+      const uint32_t qi = (qb[i] >> (4 * h)) & 15u;
+      uint32_t m = 0;
+#pragma unroll
+      for (int q = 0; q < 6; ++q) {
+        const int p = __ldg(d.nb + (size_t)i * 6 + q);
+        if (p < i) m |= spread4(~(qi ^ (qb[p] >> (4 * h))) & 15u) << q;
+      }
+      bond[i] = m;
+      lab[i] = make_uint4((uint32_t)i, (uint32_t)i, (uint32_t)i, (uint32_t)i);
+    }
+    __syncthreads();
+    for (;;) {
+      int hooked = 0;
+      for (int i = threadIdx.x; i < V; i += blockDim.x) {
+        const uint32_t m = bond[i];
+        if (!m) continue;
+        const uint4 li4 = lab[i];
+        const uint32_t li[4] = {li4.x, li4.y, li4.z, li4.w};
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+          const uint32_t mq = (m >> q) & 0x01010101u;
+          if (!mq) continue;
+          const int p = __ldg(d.nb + (size_t)i * 6 + q);
+          const uint4 lj4 = lab[p];
+          const uint32_t lj[4] = {lj4.x, lj4.y, lj4.z, lj4.w};
+#pragma unroll
+          for (int l = 0; l < 4; ++l)
+            if (((mq >> (8 * l)) & 1u) && lj[l] != li[l]) {
+              atomicMin(&lab1[4 * (size_t)max(li[l], lj[l]) + l], min(li[l], lj[l]));
+              hooked = 1;
+            }
+        }
+      }
+      if (!__syncthreads_or(hooked)) break;
+      for (;;) {
+        int moved = 0;
+        for (int i = threadIdx.x; i < V; i += blockDim.x) {
+          const uint4 x = lab[i];
+          const uint4 y = make_uint4(lab1[4 * (size_t)x.x], lab1[4 * (size_t)x.y + 1], lab1[4 * (size_t)x.z + 2],
+                                     lab1[4 * (size_t)x.w + 3]);
+          if (y.x != x.x || y.y != x.y || y.z != x.z || y.w != x.w) { lab[i] = y; moved = 1; }
+        }
+        if (!__syncthreads_or(moved)) break;
+      }
+    }
+    // coins of the roots (bits 0..3 of the roots' bond words, no longer needed)
+    for (int i = threadIdx.x; i < V; i += blockDim.x) {
+      const uint4 x = lab[i];
+      const uint32_t xs[4] = {x.x, x.y, x.z, x.w};
+      uint32_t c = 0;
+#pragma unroll
+      for (int l = 0; l < 4; ++l) {
+        if (xs[l] != (uint32_t)i) continue;
+        const int lane = grp * 8 + 4 * h + l;
+        const uint32_t tag = (((uint32_t)(w * 64 + lane) << 6 | (uint32_t)b) << 1) | (uint32_t)g;
+        uint32_t v0 = (uint32_t)mv, v1 = (uint32_t)(mv >> 32), v2 = (uint32_t)i, v3 = tag;
+        philox10(v0, v1, v2, v3, (uint32_t)key, (uint32_t)(key >> 32));
+        c |= (v0 & 1u) << l;
+      }
+      bond[i] = c;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < V; i += blockDim.x) {
+      const uint4 x = lab[i];
+      const uint32_t f = (bond[x.x] & 1u) | (bond[x.y] & 2u) | (bond[x.z] & 4u) | (bond[x.w] & 8u);
+      fb[i] |= (uint8_t)(f << (4 * h));
+    }
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < V; i += blockDim.x) Qb[(size_t)i * 8] = fb[i];
+}
+
 // Both replicas of the group take the flip words: thread per (word, site, slot).
 __device__ __forceinline__ void sp_flip_body(const SpDev &d, int g, long long t) {
   const int V = d.V, nc = d.nclust;
@@ -551,9 +652,10 @@ __global__ void kb_sp_overlap(const __grid_constant__ SpBatchDev b, int g) {
   sp_overlap_body(d, g, (long long)blk * blockDim.x + threadIdx.x);
 }
 __global__ void __launch_bounds__(1024) kb_sp_cluster(const __grid_constant__ SpBatchDev b, int g) {
-  extern __shared__ uint32_t sm[];
+  extern __shared__ __align__(16) uint32_t sm[];
   SPB_ITEM(SPB_CL0 + g)
-  sp_cluster_body(d, g, blk, sm);
+  if (d.V <= kSpCluster4MaxV) sp_cluster4_body(d, g, blk, sm);
+  else sp_cluster_body(d, g, blk, sm);
 }
 __global__ void kb_sp_flip(const __grid_constant__ SpBatchDev b, int g) {
   SPB_ITEM(SPB_FL0 + g)
@@ -585,7 +687,7 @@ cudaError_t sp_batch_setup() {
   cudaError_t e = cudaFuncSetAttribute(kb_sp_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(kb_sp_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)sp_cluster_smem(kSpClusterMaxV));
+                             (int)std::max(sp_cluster_smem(kSpClusterMaxV), sp_cluster_smem(kSpCluster4MaxV)));
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(kb_sp_permute, cudaFuncAttributeMaxDynamicSharedMemorySize, kPermRows * 64 * 8);
   return e;
@@ -651,8 +753,9 @@ __global__ void k_sp_overlap(const __grid_constant__ SpDev d, int g) {
   sp_overlap_body(d, g, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 __global__ void __launch_bounds__(1024) k_sp_cluster(const __grid_constant__ SpDev d, int g) {
-  extern __shared__ uint32_t sm[];
-  sp_cluster_body(d, g, blockIdx.x, sm);
+  extern __shared__ __align__(16) uint32_t sm[];
+  if (d.V <= kSpCluster4MaxV) sp_cluster4_body(d, g, blockIdx.x, sm);
+  else sp_cluster_body(d, g, blockIdx.x, sm);
 }
 __global__ void k_sp_flip(const __grid_constant__ SpDev d, int g) {
   sp_flip_body(d, g, (long long)blockIdx.x * blockDim.x + threadIdx.x);
@@ -688,7 +791,7 @@ cudaError_t sp_setup() {
   cudaError_t e = cudaFuncSetAttribute(k_sp_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_sp_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)sp_cluster_smem(kSpClusterMaxV));
+                             (int)std::max(sp_cluster_smem(kSpClusterMaxV), sp_cluster_smem(kSpCluster4MaxV)));
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_sp_permute, cudaFuncAttributeMaxDynamicSharedMemorySize, kPermRows * 64 * 8);
   return e;
@@ -725,7 +828,9 @@ cudaError_t sp_launch_permute(const SpDev &d, cudaStream_t st) {
 }
 
 
-size_t sp_cluster_smem(int V) { return V <= kSpClusterMaxV ? (size_t)V * 7 : 0; }
+size_t sp_cluster_smem(int V) {
+  return V <= kSpCluster4MaxV ? (size_t)V * 22 : V <= kSpClusterMaxV ? (size_t)V * 7 : 0;
+}
 
 // Block size of the cluster labelling: 1024 threads, 256 for lattices of
 // at most 2048 sites (256 threads measured 20 % slower on 6912 sites, 512 the
