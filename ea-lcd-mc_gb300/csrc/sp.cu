@@ -606,14 +606,21 @@ __device__ __forceinline__ int spb_job(const uint32_t *pre, int n, uint32_t v) {
   return lo;
 }
 
+// The block's job descriptor is copied to SMEM once (SMEM cannot alias the
+// job's global arrays, and a per-thread copy would go to the stack).
 #define SPB_ITEM(KIND)                                        \
+  __shared__ SpDev s_job;                                     \
   const uint32_t *pre_ = b.pre[KIND];                         \
   const int jb = spb_job(pre_, b.njobs, blockIdx.x);          \
-  const SpDev d = b.jobs[jb];  /* a copy: no aliasing with the job's arrays */ \
+  if (threadIdx.x == 0) s_job = b.jobs[jb];                   \
+  __syncthreads();                                            \
+  const SpDev &d = s_job;                                     \
   const int blk = (int)(blockIdx.x - __ldg(pre_ + jb));
 
 __global__ void kb_sp_fill(const __grid_constant__ SpBatchDev b, int colour) {
-  const SpDev d = b.jobs[blockIdx.x];
+  __shared__ SpDev d;
+  if (threadIdx.x == 0) d = b.jobs[blockIdx.x];
+  __syncthreads();
   if (colour < d.ncol) sp_fill_body(d);
 }
 __global__ void __launch_bounds__(512) kb_sp_pass(const __grid_constant__ SpBatchDev b, int colour) {
@@ -683,13 +690,19 @@ void sp_batch_blocks(const SpDev &d, bool cluster, uint32_t out[SPB_COUNT]) {
   }
 }
 
+// Largest dynamic SMEM of a kernel: the 227 KB of a block less its static SMEM.
+template <class K>
+static cudaError_t max_dynamic_smem(K kernel) {
+  cudaFuncAttributes fa;
+  cudaError_t e = cudaFuncGetAttributes(&fa, kernel);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024 - (int)fa.sharedSizeBytes);
+}
+
 cudaError_t sp_batch_setup() {
-  cudaError_t e = cudaFuncSetAttribute(kb_sp_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(kb_sp_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)std::max(sp_cluster_smem(kSpClusterMaxV), sp_cluster_smem(kSpCluster4MaxV)));
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(kb_sp_permute, cudaFuncAttributeMaxDynamicSharedMemorySize, kPermRows * 64 * 8);
+  cudaError_t e = max_dynamic_smem(kb_sp_pass);
+  if (e == cudaSuccess) e = max_dynamic_smem(kb_sp_cluster);
+  if (e == cudaSuccess) e = max_dynamic_smem(kb_sp_permute);
   return e;
 }
 
@@ -780,9 +793,10 @@ size_t sp_sweep_smem(int NB, int NR, int kt) {
 int sp_kt(int NB, int NR, int nsites_colour) {
   int kt = 1;
   while (kt < 64 && NB * kt * NR < 256) kt <<= 1;
-  while (kt > 1 && sp_sweep_smem(NB, NR, kt) > 227 * 1024) kt >>= 1;
-  if (sp_sweep_smem(NB, NR, kt) > 227 * 1024) return 0;
-  while (kt < 64 && sp_sweep_smem(NB, NR, 2 * kt) <= 227 * 1024 && (nsites_colour + 2 * kt - 1) / (2 * kt) >= 2 * 152)
+  const size_t lim = 227 * 1024 - 512;  // room for the batched kernels' static SMEM
+  while (kt > 1 && sp_sweep_smem(NB, NR, kt) > lim) kt >>= 1;
+  if (sp_sweep_smem(NB, NR, kt) > lim) return 0;
+  while (kt < 64 && sp_sweep_smem(NB, NR, 2 * kt) <= lim && (nsites_colour + 2 * kt - 1) / (2 * kt) >= 2 * 152)
     kt <<= 1;
   return kt;
 }

@@ -79,8 +79,8 @@ struct SpDev {
 // a global scratch region of sp_cluster_words(V) words per CTA.
 constexpr int kSpClusterMaxV = 32768;
 // Lattices up to this size are labelled 4 samples at a time (22 bytes of
-// SMEM per site).
-constexpr int kSpCluster4MaxV = 10560;
+// SMEM per site; 512 bytes left for static SMEM).
+constexpr int kSpCluster4MaxV = 10500;
 __host__ __device__ inline size_t sp_cluster_words(int V) { return ((size_t)V * 7 + 15) / 16 * 4; }
 
 int sp_kt(int NB, int NR, int nsites_colour);
