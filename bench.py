@@ -623,6 +623,8 @@ def main():
     ap.add_argument("--no-mixed", action="store_true", help="skip the batched vs plain mixed-geometry leg")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving (Poisson stream) leg")
     ap.add_argument("--no-sp", action="store_true", help="skip the sample-packed legs")
+    ap.add_argument("--mix-only", default="", choices=["", "plain", "batched"],
+                    help="only two bins of the 36-job x 32-sample multispin mix in this form (for profilers)")
     ap.add_argument("--rng-sms", type=int, default=-1,
                     help="SMs of the cluster-uniform generator's partition for the headline job (-1: automatic)")
     ap.add_argument("--sp-case", default="", help="run only the sample-packed workloads whose name contains this "
@@ -636,6 +638,24 @@ def main():
         torch.distributed.init_process_group("nccl" if args.impl == "ours" else "gloo")
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.mix_only:
+        eagb = load_eagb()
+        jobs = mixed_jobs(eagb, local, 32, 1)
+        cad = dict(itmax=1, houfr=MIX_HOUFR, mesfr=1, ptfr=1)
+        if args.mix_only == "batched":
+            batch = eagb.Batch(jobs)
+            for _ in range(2):
+                batch.run_bin(**cad)
+            batch.sync()
+            batch.close()
+        else:
+            for _ in range(2):
+                for j in jobs:
+                    j.run_cycles(**cad)
+            for j in jobs:
+                j.sync()
+        for j in jobs:
+            j.close()
     elif args.sp_case:
         import torch
         print(json.dumps(run_sp(args, local, torch, load_eagb())), flush=True)
