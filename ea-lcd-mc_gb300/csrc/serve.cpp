@@ -90,6 +90,7 @@ struct Group {
   ClassKey key;
   ea_cadence cad{};
   int NR = 0;
+  bool packed = false;  // a solo group of sample-packed jobs, one at a time
   Job *solo = nullptr;
   ea_batch *batch = nullptr;
   std::vector<Job *> members;
@@ -195,12 +196,13 @@ Group *group_for(ea_server *s, Job *j) {
   const ClassKey key{j->req.geom.nrep, c.itmax, c.houfr, c.mesfr, c.ptfr, c.cluster, c.nclust};
   if (!j->packed())
     for (auto &g : s->groups)
-      if (!g->solo && g->key == key) return g.get();
+      if (!g->packed && g->key == key) return g.get();
   if (j->packed()) {
-    // a finished solo group whose bins have all ended is reused
+    // a solo group whose job has finished and whose bins have all ended is reused
     for (auto &g : s->groups)
-      if (g->solo && g->members.empty() && g->inflight.empty()) {
+      if (g->packed && !g->solo && g->members.empty() && g->inflight.empty()) {
         g->solo = j;
+        g->key = key;
         g->cad = c;
         g->NR = j->req.geom.nrep;
         return g.get();
@@ -208,6 +210,7 @@ Group *group_for(ea_server *s, Job *j) {
   }
   s->groups.emplace_back(new Group());
   Group *g = s->groups.back().get();
+  g->packed = j->packed();
   if (j->packed()) g->solo = j;
   g->key = key;
   g->cad = c;
@@ -385,6 +388,7 @@ bool step_group(ea_server *s, Group *g) {
       s->to_free.push_back(j);
     }
     g->members.clear();
+    g->solo = nullptr;
     if (g->batch) { ea_batch_destroy(g->batch); g->batch = nullptr; }
     s->cv.notify_all();
     return false;
