@@ -163,11 +163,36 @@ def mixed_jobs(eagb, dev, ns, copies):
     return jobs
 
 
+def timed_sequential(torch, dev, jobs, enqueue_one, steps, join=None):
+    """The plain form run one geometry after another: each job's bin starts
+    when the previous job's bin has ended (device-side ordering through events,
+    no host synchronisation); CUDA-event time in ms."""
+    s0 = torch.cuda.Stream(device=dev)
+    streams = [torch.cuda.ExternalStream(j.stream(), device=dev) for j in jobs]
+    torch.cuda.synchronize(dev)
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record(s0)
+    prev = t0
+    for _ in range(steps):
+        for j, st in zip(jobs, streams):
+            st.wait_event(prev)
+            enqueue_one(j)
+            if join:
+                join(j)
+            prev = torch.cuda.Event()
+            prev.record(st)
+    s0.wait_event(prev)
+    t1.record(s0)
+    torch.cuda.synchronize(dev)
+    return t0.elapsed_time(t1)
+
+
 def run_mixed(args, dev, torch, eagb, ns, copies):
     """Batched persistent form vs plain form (one job per launch sequence, every
-    job on its own stream, all enqueued before waiting) on the same mixed
-    workload, from twin initial states; one step = one bin of itmax=1 for
-    every job.  Inputs (spins + uniforms) are far larger than L2."""
+    job on its own stream, all enqueued before waiting; and the same jobs one
+    geometry after another) on the same mixed workload, from twin initial
+    states; one step = one bin of itmax=1 for every job.  Inputs (spins +
+    uniforms) are far larger than L2."""
     su_step = 0
     plain, batched = mixed_jobs(eagb, dev, ns, copies), mixed_jobs(eagb, dev, ns, copies)
     for j in plain:
@@ -214,12 +239,17 @@ def run_mixed(args, dev, torch, eagb, ns, copies):
         same = same and np.array_equal(a.bin_results()[0], b.bin_results()[0])
     tile = batch.tile()
     batch.close()
+    # the same plain jobs, one geometry after another (after the check)
+    seq_steps = max(1, args.steps // 4)
+    ms_seq = timed_sequential(torch, dev, plain, lambda j: j.run_cycles(**cad), seq_steps, join=lambda j: j.join())
     for j in plain + batched:
         j.close()
     vp = su_step * args.steps / (ms_plain * 1e-3) / 1e12
     vb = su_step * args.steps / (ms_batch * 1e-3) / 1e12
+    vs = su_step * seq_steps / (ms_seq * 1e-3) / 1e12
     return {"workload": MIX_WORKLOAD % ns, "jobs": len(plain), "unit": "spin-updates/ps",
             "plain_value": vp, "batched_value": vb, "speedup": vb / vp,
+            "plain_sequential_value": vs, "speedup_vs_sequential": vb / vs,
             "plain_ms_per_step": ms_plain / args.steps, "batched_ms_per_step": ms_batch / args.steps,
             "spin_updates_per_step": su_step, "bit_exact_plain_vs_batched": bool(same), "tile": tile,
             "graph": "sweep/energy/tempering cycle replayed as a CUDA graph",
@@ -454,12 +484,16 @@ def run_mixed_sp(args, dev, torch, eagb, nwords=SPMIX_WORDS, steps=2):
     ms_batch = timed(bstreams, batch_step, steps)
     same = all(np.array_equal(a.get_spins(), b.get_spins()) for a, b in zip(plain, batched))
     batch.close()
+    # the same plain jobs, one geometry after another (after the check)
+    ms_seq = timed_sequential(torch, dev, plain, lambda j: j.run_async(**cad), steps)
     for j in plain + batched:
         j.close()
     vp = su_step * steps / (ms_plain * 1e-3) / 1e12
     vb = su_step * steps / (ms_batch * 1e-3) / 1e12
+    vs = su_step * steps / (ms_seq * 1e-3) / 1e12
     return {"workload": SPMIX_WORKLOAD % nwords, "jobs": len(plain), "samples": 64 * nwords, "unit": "spin-updates/ps",
             "plain_value": vp, "batched_value": vb, "speedup": vb / vp, "plain_ms_per_step": ms_plain / steps,
+            "plain_sequential_value": vs, "speedup_vs_sequential": vb / vs,
             "batched_ms_per_step": ms_batch / steps, "spin_updates_per_step": su_step,
             "bit_exact_plain_vs_batched": bool(same),
             "graph": "one bin iteration of the batch replayed as a CUDA graph",
