@@ -66,9 +66,11 @@ __device__ __forceinline__ void sp_pass_body(const SpDev &d, int off, int n, int
     s_nb[i] = v;
   }
   __syncthreads();
+  // random words at [site of the tile][replica][slot]: the update phase's
+  // consecutive lanes (consecutive slots) then read consecutive words
   const int plane = NB * kt * NR;
   for (int t = tid; t < plane; t += nth) {
-    const int r = t % NR, kk = (t / NR) % kt, b = t / (NR * kt);
+    const int b = t % NB, r = (t / NB) % NR, kk = t / (NB * NR);
     if (k0 + kk >= n) continue;
     const int site = s_nb[kk * 7];
     const uint32_t tp = (uint32_t)(((size_t)b * V + site) * NR + r);
@@ -106,7 +108,7 @@ __device__ __forceinline__ void sp_pass_body(const SpDev &d, int off, int n, int
       u64 f[6];
 #pragma unroll
       for (int q = 0; q < 6; ++q) f[q] = sv ^ __ldg(Jp + q) ^ Sw[(size_t)sn[q + 1] * G];
-      const int o = (b * kt + kk) * NR + r;
+      const int o = (kk * NR + r) * NB + b;
       Sw[(size_t)site * G] = sv ^ flip_mask(f, s_rnd[o], s_rnd[plane + o], s_rnd[2 * plane + o]);
       for (kk += step; kk >= nk; kk -= nk) ++w;
     }
@@ -250,13 +252,19 @@ __device__ __forceinline__ void sp_permute_body(const SpDev &d, int blk, u64 *ro
   const long long r0 = (long long)blk * kPermRows;
   if (blk == 0 && threadIdx.x == 0) *d.ptstep += 1ull;
   const int nr = (int)min((long long)kPermRows, nrows - r0);
+  // rows sit in SMEM with an odd stride (in words): the threads' scans then
+  // hit distinct banks (an even stride such as NB = 24 is a 16-way conflict)
+  const int rs = NB | 1;
   u64 *g = d.S + (size_t)r0 * NB;
-  for (int k = threadIdx.x; k < nr * NB; k += blockDim.x) rows[k] = g[k];
+  for (int k = threadIdx.x; k < nr * NB; k += blockDim.x) {
+    const int row = k / NB;
+    rows[row * rs + (k - row * NB)] = g[k];
+  }
   __syncthreads();
   if (threadIdx.x < nr) {
     const long long t = r0 + threadIdx.x;
     const int r = (int)(t % NR), w = (int)(t / ((long long)NR * d.V));
-    u64 *p = rows + (size_t)threadIdx.x * NB;
+    u64 *p = rows + (size_t)threadIdx.x * rs;
     const u64 *M = d.M + ((size_t)w * NR + r) * (NB - 1);
     u64 cur = p[0];
     for (int i = 0; i < NB - 1; ++i) {
@@ -269,7 +277,10 @@ __device__ __forceinline__ void sp_permute_body(const SpDev &d, int blk, u64 *ro
     p[NB - 1] = cur;
   }
   __syncthreads();
-  for (int k = threadIdx.x; k < nr * NB; k += blockDim.x) g[k] = rows[k];
+  for (int k = threadIdx.x; k < nr * NB; k += blockDim.x) {
+    const int row = k / NB;
+    g[k] = rows[row * rs + (k - row * NB)];
+  }
 }
 
 
@@ -807,7 +818,7 @@ cudaError_t sp_setup() {
     e = cudaFuncSetAttribute(k_sp_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)std::max(sp_cluster_smem(kSpClusterMaxV), sp_cluster_smem(kSpCluster4MaxV)));
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_sp_permute, cudaFuncAttributeMaxDynamicSharedMemorySize, kPermRows * 64 * 8);
+    e = cudaFuncSetAttribute(k_sp_permute, cudaFuncAttributeMaxDynamicSharedMemorySize, kPermRows * 65 * 8);
   return e;
 }
 
@@ -837,7 +848,7 @@ cudaError_t sp_launch_pt(const SpDev &d, cudaStream_t st) {
 
 cudaError_t sp_launch_permute(const SpDev &d, cudaStream_t st) {
   const long long n = (long long)d.nw * d.V * d.NR;
-  k_sp_permute<<<(unsigned)((n + kPermRows - 1) / kPermRows), kPermRows, (size_t)kPermRows * d.NB * 8, st>>>(d);
+  k_sp_permute<<<(unsigned)((n + kPermRows - 1) / kPermRows), kPermRows, (size_t)kPermRows * (d.NB | 1) * 8, st>>>(d);
   return cudaGetLastError();
 }
 
@@ -1388,7 +1399,7 @@ static int spb_upload(SpClass &k, bool cluster, cudaStream_t bs) {
     sp_batch_blocks(hj[i], cluster, cnt);
     for (int q = 0; q < SPB_COUNT; ++q) hp[(size_t)q * (n + 1) + i + 1] = hp[(size_t)q * (n + 1) + i] + cnt[q];
     pass_smem = std::max(pass_smem, (int)sp_sweep_smem(hj[i].NB, hj[i].NR, hj[i].kt));
-    perm_smem = std::max(perm_smem, kPermRows * hj[i].NB * 8);
+    perm_smem = std::max(perm_smem, kPermRows * (hj[i].NB | 1) * 8);
     if (cluster) cl_smem = std::max(cl_smem, (int)sp_cluster_smem(hj[i].V));
   }
   if (k.up_jobs.size() != hj.size() || std::memcmp(k.up_jobs.data(), hj.data(), sizeof(SpDev) * n) ||
