@@ -93,6 +93,44 @@ __device__ __forceinline__ void sp_pass_body(const SpDev &d, int off, int n, int
   const int G = NR * NB;
   const size_t wps = (size_t)V * G;  // words per sample word
   const int nk = min(kt, n - k0), nidx = nk * d.nw;
+  if ((NB & 1) == 0) {
+    // even NB: a lane takes two adjacent slots of a (replica, site) with
+    // 16-byte loads and stores (every word offset here is even)
+    const int G2 = G >> 1, NB2 = NB >> 1;
+    const size_t wps2 = wps >> 1;
+    for (int lg = tid % G2, grp = tid / G2, ngrp = max(1, nth / G2); lg < G2; lg += (nth >= G2 ? G2 : nth)) {
+      if (nth >= G2 && grp >= ngrp) break;
+      const int b = 2 * (lg % NB2), r = lg / NB2;
+      ulonglong2 *Sc = reinterpret_cast<ulonglong2 *>(d.S + r * NB + b);
+      const int step = nth >= G2 ? ngrp : 1;
+      int idx = nth >= G2 ? grp : 0, kk = idx % nk, w = idx / nk;
+      for (; idx < nidx; idx += step) {
+        const int *sn = s_nb + kk * 7;
+        const int site = sn[0];
+        ulonglong2 *Sw = Sc + (size_t)w * wps2;
+        const u64 *Jp = d.J + ((size_t)w * V + site) * 6;
+        const ulonglong2 sv = Sw[(size_t)site * G2];
+        u64 f0[6], f1[6];
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+          const u64 jq = __ldg(Jp + q);
+          const ulonglong2 nq = Sw[(size_t)sn[q + 1] * G2];
+          f0[q] = sv.x ^ jq ^ nq.x;
+          f1[q] = sv.y ^ jq ^ nq.y;
+        }
+        const int o = (kk * NR + r) * NB + b;
+        const ulonglong2 r0 = *reinterpret_cast<const ulonglong2 *>(s_rnd + o);
+        const ulonglong2 r1 = *reinterpret_cast<const ulonglong2 *>(s_rnd + plane + o);
+        const ulonglong2 r2 = *reinterpret_cast<const ulonglong2 *>(s_rnd + 2 * plane + o);
+        ulonglong2 out;
+        out.x = sv.x ^ flip_mask(f0, r0.x, r1.x, r2.x);
+        out.y = sv.y ^ flip_mask(f1, r0.y, r1.y, r2.y);
+        Sw[(size_t)site * G2] = out;
+        for (kk += step; kk >= nk; kk -= nk) ++w;
+      }
+    }
+    return;
+  }
   for (int lg = tid % G, grp = tid / G, ngrp = max(1, nth / G); lg < G; lg += (nth >= G ? G : nth)) {
     if (nth >= G && grp >= ngrp) break;
     const int b = lg % NB, r = lg / NB;

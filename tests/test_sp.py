@@ -182,13 +182,19 @@ class OracleSP:
 
 
 def new_job(L, Lz, bc, lutname, NR, nw, jobid=3):
-    betas, cum = lut(lutname)
+    # "name:k" takes the first k temperatures of a set (odd NB runs the
+    # pass's one-slot-per-lane path, even NB the two-slot one)
+    name, _, k = lutname.partition(":")
+    betas, cum = lut(name)
+    if k:
+        betas, cum = betas[:int(k)], cum[:int(k)]
     job = eagb.SpJob(L, Lz, betas, cum, nrep=NR, nwords=nw, bc=bc, seeds=SEEDS, jobid=jobid)
     job.cum = np.ascontiguousarray(cum, np.uint64)
     return job
 
 
 CASES = [(6, 8, eagb.EA_PBC, "T08_16_N4", 2, 2), (5, 7, eagb.EA_OBC, "T07_16_N6", 3, 1),
+         (6, 6, eagb.EA_OBC, "T07_16_N6:5", 3, 2), (7, 4, eagb.EA_PBC, "T07_16_N8:7", 2, 1),
          (3, 3, eagb.EA_PBC, "T07_16_N8", 2, 1), (12, 16, eagb.EA_OBC, "T07_16_N12", 4, 1),
          (8, 16, eagb.EA_OBC, "T07_16_N24", 2, 3)]
 
