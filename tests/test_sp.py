@@ -76,6 +76,19 @@ def test_graph(L, Lz, bc):
             assert np.array_equal(nb[bot & corner, 5], site(x, y, Lz - 1)[bot & corner])
 
 
+def test_colour_counts_all_small_tubes():
+    """Every tube with L, Lz in 2..13 under PBC and OBC takes 2 colours when
+    bipartite and 3 otherwise (the greedy fallback is never needed), and
+    each colouring is proper."""
+    for L in range(2, 14):
+        for Lz in range(2, 14):
+            for bc in (eagb.EA_PBC, eagb.EA_OBC):
+                nb, mate, col, ncol = eagb.sp_graph(L, Lz, bc)
+                bip = L % 2 == 0 and (bc == eagb.EA_OBC or Lz % 2 == 0)
+                assert ncol == (2 if bip else 3), (L, Lz, bc, ncol)
+                assert np.all(col[nb] != col[:, None])
+
+
 def test_couplings_and_spins():
     g = eagb.SpGeom(5, 7, 4, 3, 2, eagb.EA_OBC)
     nb, mate, col, ncol = eagb.sp_graph(5, 7, eagb.EA_OBC)
