@@ -454,6 +454,15 @@ def sp_graph(L, Lz, bc):
     return nb, mate, col, n.value
 
 
+def sp_job_bytes(g, cad=None, betas=None):
+    """Device bytes of a sample-packed job (ea_sp_job_bytes)."""
+    out = C.c_uint64()
+    b = None if betas is None else np.ascontiguousarray(betas, np.float64)
+    _ck(lib().ea_sp_job_bytes(C.byref(g), None if cad is None else C.byref(cad), None if b is None else P(b),
+                              C.byref(out)))
+    return out.value
+
+
 def sp_host_init(g, seed_J, seed_u):
     V = g.L * g.L * g.Lz
     J = np.zeros((g.nwords, V, 6), np.uint64)

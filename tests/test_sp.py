@@ -103,6 +103,22 @@ def test_couplings_and_spins():
     assert np.array_equal(J, J2) and np.array_equal(S, S2)
 
 
+def test_job_bytes_cover_the_arrays():
+    """What admission charges for a sample-packed job covers its spins,
+    couplings and, with cluster moves, the overlap words (and the global
+    labelling scratch of lattices above 32768 sites)."""
+    betas, _ = lut("T07_16_N24")
+    for L, Lz, nw, NR in [(12, 48, 4, 4), (7, 9, 1, 2), (20, 96, 2, 2)]:
+        g = eagb.SpGeom(L, Lz, 24, NR, nw, eagb.EA_OBC)
+        V = L * L * Lz
+        plain = eagb.sp_job_bytes(g, eagb.Cadence(2, 10, 1, 1, 0, 0), betas)
+        clus = eagb.sp_job_bytes(g, eagb.Cadence(2, 10, 1, 1, 1, 0), betas)
+        assert plain >= nw * V * NR * 24 * 8 + nw * V * 48
+        assert clus - plain >= nw * 12 * V * 8 + (nw * 12 * 8 * 7 * V if V > 32768 else 0)
+    with pytest.raises(eagb.EAError):
+        eagb.sp_job_bytes(eagb.SpGeom(1, 4, 24, 2, 1, eagb.EA_PBC))
+
+
 def brute_dos(nb, J, lane):
     """Plain enumeration from the definition: E = 3V - (unsatisfied half-edges)."""
     V = nb.shape[0]
