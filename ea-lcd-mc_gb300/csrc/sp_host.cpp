@@ -3,6 +3,7 @@
 // proper colouring, and the seeded couplings and initial spins.
 #include <algorithm>
 #include <cstring>
+#include <thread>
 
 #include "host.hpp"
 #include "sp.cuh"
@@ -150,6 +151,23 @@ ea_xoshiro word_stream(uint64_t seed, int w) {
   for (int k = 0; k < 4; ++k) x.s[k] = splitmix64(sm);
   return x;
 }
+
+// Runs f(w) for w = 0..n-1 on up to 16 host threads (each word has its own
+// stream, so the order does not matter).
+template <class F>
+void for_words(int n, F f) {
+  const int nth = std::max(1, std::min({n, 16, (int)std::thread::hardware_concurrency()}));
+  if (nth == 1) {
+    for (int w = 0; w < n; ++w) f(w);
+    return;
+  }
+  std::vector<std::thread> pool;
+  for (int t = 0; t < nth; ++t)
+    pool.emplace_back([=] {
+      for (int w = t; w < n; w += nth) f(w);
+    });
+  for (auto &th : pool) th.join();
+}
 }  // namespace
 
 // Couplings [w][site][slot]: every bit is one sample's +-J (bit 1 = the bond
@@ -157,20 +175,20 @@ ea_xoshiro word_stream(uint64_t seed, int w) {
 // (site, slot) order; the first end of each bond draws its word, the other
 // end copies it.
 void sp_couplings(const SpGraph &g, int nwords, uint64_t seed_J, uint64_t *J) {
-  for (int w = 0; w < nwords; ++w) {
+  for_words(nwords, [&g, seed_J, J](int w) {
     ea_xoshiro x = word_stream(seed_J, w);
     uint64_t *Jw = J + (size_t)w * g.V * 6;
     for (int h = 0; h < 6 * g.V; ++h) Jw[h] = g.mate[h] > h ? xo_next(x) : Jw[g.mate[h]];
-  }
+  });
 }
 
 // Initial spins [w][site][rep][slot], one word per draw in that order.
 void sp_spins(const SpGraph &g, int nwords, int NR, int NB, uint64_t seed_u, uint64_t *S) {
   const size_t per = (size_t)g.V * NR * NB;
-  for (int w = 0; w < nwords; ++w) {
+  for_words(nwords, [per, seed_u, S](int w) {
     ea_xoshiro x = word_stream(seed_u, w);
     for (size_t i = 0; i < per; ++i) S[(size_t)w * per + i] = xo_next(x);
-  }
+  });
 }
 
 }  // namespace eagb

@@ -101,6 +101,13 @@ def test_couplings_and_spins():
     assert abs(bits - 0.5) < 0.01
     J2, S2 = eagb.sp_host_init(g, 11, 22)
     assert np.array_equal(J, J2) and np.array_equal(S, S2)
+    # the streams themselves are pinned: words may be generated in any order
+    # or in parallel, never differently
+    import hashlib
+    g5 = eagb.SpGeom(5, 7, 4, 3, 5, eagb.EA_OBC)
+    J5, S5 = eagb.sp_host_init(g5, 11, 22)
+    assert hashlib.sha256(J5.tobytes()).hexdigest()[:32] == "6b126edd8f1b964dcf3b91481282f69d"
+    assert hashlib.sha256(S5.tobytes()).hexdigest()[:32] == "a92dd8c263255d4ffc91f5dad7cc45d7"
 
 
 def test_job_bytes_cover_the_arrays():
