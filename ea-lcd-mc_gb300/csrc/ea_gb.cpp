@@ -97,11 +97,19 @@ void create_error(const char *fmt, ...) {
   delete_running();
 }
 
+// The reference's handler writes <dir>/error and exits 1 (io.c:894-918).  The
+// signal can interrupt a CUDA runtime call that holds the runtime's locks, so
+// the process ends with _exit after flushing its streams: exit() would run the
+// runtime's teardown from inside the handler, which can wait on those locks
+// for ever.  The driver releases the device when the process ends.
 void stop_run(int sig) {
   if (sig == SIGTERM) create_error("Received SIGTERM\n");
   if (sig == SIGINT) create_error("Received SIGINT\n");
   if (sig == SIGUSR1) create_error("Received SIGUSR1\n");
-  print_and_exit("Aborting programma (SIGNAL=%d)\n", sig);
+  fprintf(stderr, "Aborting programma (SIGNAL=%d)\n", sig);
+  fflush(stdout);
+  fflush(stderr);
+  _exit(1);
 }
 
 void ignore_sigterm() { signal(SIGTERM, SIG_IGN); signal(SIGINT, SIG_IGN); signal(SIGUSR1, SIG_IGN); }

@@ -61,10 +61,24 @@ void or_sp_pass(int V, int NR, int NB, int nw, const int32_t *nb, const int32_t 
   }
 }
 
-/* Unsatisfied half-edges per (word, sample, replica, slot): U2 [nw][64][NR][NB]. */
+/* Unsatisfied half-edges per (word, sample, replica, slot): U2 [nw][64][NR][NB].
+ * Per-sample counts of the unsatisfied slots f of every site: each byte of f
+ * adds the 0/1 counts of its 8 samples to one 64-bit accumulator (8 bytes,
+ * one per sample) through a table, flushed into int32 counters before a
+ * byte can overflow. */
 void or_sp_energy(int V, int NR, int NB, int nw, const int32_t *nb, const uint64_t *J, const uint64_t *S,
                   int32_t *U2) {
   const size_t G = (size_t)NR * NB;
+  static uint64_t spread[256];
+  static int spread_done = 0;
+  if (!spread_done) {
+    for (int x = 0; x < 256; x++) {
+      uint64_t v = 0;
+      for (int b = 0; b < 8; b++) v |= (uint64_t)((x >> b) & 1) << (8 * b);
+      spread[x] = v;
+    }
+    spread_done = 1;
+  }
   memset(U2, 0, sizeof(int32_t) * (size_t)nw * 64 * G);
 #pragma omp parallel for schedule(static)
   for (int wo = 0; wo < nw * (int)G; wo++) {
@@ -72,12 +86,24 @@ void or_sp_energy(int V, int NR, int NB, int nw, const int32_t *nb, const uint64
     const uint64_t *Sw = S + (size_t)w * V * G;
     const uint64_t *Jw = J + (size_t)w * V * 6;
     int32_t cnt[64];
+    uint64_t acc[8];
     memset(cnt, 0, sizeof(cnt));
-    for (int i = 0; i < V; i++)
+    memset(acc, 0, sizeof(acc));
+    int pending = 0;
+    for (int i = 0; i < V; i++) {
       for (int d = 0; d < 6; d++) {
         const uint64_t f = Sw[(size_t)i * G + o] ^ Jw[(size_t)i * 6 + d] ^ Sw[(size_t)nb[i * 6 + d] * G + o];
-        for (int lane = 0; lane < 64; lane++) cnt[lane] += (int)((f >> lane) & 1ULL);
+        for (int k = 0; k < 8; k++) acc[k] += spread[(f >> (8 * k)) & 255];
       }
+      pending += 6;
+      if (pending > 240 || i == V - 1) {
+        for (int k = 0; k < 8; k++) {
+          for (int b = 0; b < 8; b++) cnt[8 * k + b] += (int32_t)((acc[k] >> (8 * b)) & 255);
+          acc[k] = 0;
+        }
+        pending = 0;
+      }
+    }
     for (int lane = 0; lane < 64; lane++) U2[((size_t)w * 64 + lane) * G + o] = cnt[lane];
   }
 }
@@ -213,11 +239,15 @@ void or_sp_cluster(int V, int NR, int NB, int nw, const int32_t *nb, int nclust,
             }
           }
           const uint32_t tag = (((uint32_t)(w * 64 + lane) << 6 | (uint32_t)b) << 1) | (uint32_t)g;
+          /* the coin of each cluster, drawn at its root (q[] is free now) */
           for (int i = 0; i < V; i++) {
-            const int r = root[i];
-            uint32_t v[4] = {(uint32_t)move, (uint32_t)(move >> 32), (uint32_t)r, tag};
+            if (root[i] != i) continue;
+            uint32_t v[4] = {(uint32_t)move, (uint32_t)(move >> 32), (uint32_t)i, tag};
             philox_pt(v, (uint32_t)key, (uint32_t)(key >> 32));
-            if (v[0] & 1u) {
+            q[i] = (uint8_t)(v[0] & 1u);
+          }
+          for (int i = 0; i < V; i++) {
+            if (q[root[i]]) {
               const uint64_t bit = 1ULL << lane;
 #pragma omp atomic
               Sw[(size_t)i * G + (size_t)r1 * NB + b] ^= bit;

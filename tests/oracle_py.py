@@ -268,9 +268,15 @@ def curand_host(seed, offset, n):
 # ---------------------------------------------------------------------------
 # Sample-packed layout (oracle/sp_oracle.c)
 # ---------------------------------------------------------------------------
+_exp_tables = {}
+
+
 def sp_exp_table(betas):
     """exp(pt) of every tempering exponent that can change a decision, with
     the host libm, per beta pair (offsets) -- dE = -2, -4, ... down to pt = -50."""
+    key = np.ascontiguousarray(betas, np.float64).tobytes()
+    if key in _exp_tables:
+        return _exp_tables[key]
     vals, off = [], []
     for i in range(len(betas) - 1):
         off.append(len(vals))
@@ -283,7 +289,8 @@ def sp_exp_table(betas):
             vals.append(math.exp(pt))
             j += 1
     off.append(len(vals))
-    return np.array(vals, np.float64), np.array(off, np.int32)
+    _exp_tables[key] = (np.array(vals, np.float64), np.array(off, np.int32))
+    return _exp_tables[key]
 
 
 def sp_pass(V, NR, NB, nw, nb, sites, ctr, keys, cum, J, S):

@@ -140,20 +140,94 @@ def test_full_bins(case):
     job.close()
 
 
-def test_houdayer_conserves_pair_energy():
-    """Cluster labels on the GPU equal the oracle's min-index roots: checked through
-    a Houdayer move with uniforms all below 0.5 (every cluster flips)."""
-    job, sim = make("L16_Lz24_STRONG")
-    job.monte_carlo(2)
-    for p in range(4):
-        ctr = O.fill_bits(sim.prc, sim.xo, sim.g.NR, p, 3)
-        sim.half_sweep(ctr, p & 1)
+def _move_pairs(job):
+    """The two replica pairs the next Houdayer move draws from random_c
+    (main.cu:408-421), replayed on a copy of the job's generator."""
+    gen, _ = job.get_generators()
+    rc = O.HQ.from_buffer_copy(bytes(memoryview(gen.rc).cast("B")))
+    out = []
+    for g in range(2):
+        r1, r2 = O.C.c_int(), O.C.c_int()
+        O.lib().or_houdayer_pair(O.C.byref(rc), job.g.nrep, g, O.C.byref(r1), O.C.byref(r2))
+        out.append((r1.value, r2.value))
+    return out
+
+
+@pytest.mark.parametrize("L,Lz,lutname,ns,rule", [(16, 24, "T07_16_N8", 4, "reference"),
+                                                  (24, 16, "T07_16_N8", 8, "exact")])
+def test_houdayer_conserves_pair_energy(L, Lz, lutname, ns, rule):
+    """One Houdayer move flips each cluster of equal overlap in both replicas
+    of a pair, so E(r1) + E(r2) of every (sample, temperature < nclust,
+    group) is unchanged, every other energy is untouched, and some energies
+    do change.  Under the reference's bond rule this holds when L is a power
+    of two; at L = 24 the reference tests site 0's x-wrap bond against
+    x = 15 (HoudayerXEA.cu:96), which can split a cluster (rarely: only when
+    no other path joins its two pieces) -- with EA_CLUSTER_EXACT it holds for
+    every L.  (The reference rule at L = 24 is pinned against the oracle by
+    the whole-bin tests.)"""
+    betas, cum = lut(lutname)
+    job = eagb.new_job(L, Lz, betas, cum, nsamples=ns, bc=O.OBC, masters=MASTERS, iter0=0, jobid=3)
+    if rule == "exact":
+        eagb._ck(eagb.lib().ea_set_cluster_rule(job.ctx, 1))
+    job.monte_carlo(3)
+    job.parallel_tempering()
     E0 = job.measure_energy()
+    wctb, _ = job.get_permutations()
+    pairs = _move_pairs(job)
     job.houdayer()
     E1 = job.measure_energy()
-    # E(r1) + E(r2) is conserved per beta for both groups
-    wctb, _ = job.get_permutations()
-    assert E0.sum() == E1.sum()
+    NB, NR = job.g.nbetas, job.g.nrep
+    nclust = int(np.floor(0.5 * NB + 0.5))
+    moved = np.zeros(E0.shape, bool)
+    bad = 0
+    for r1, r2 in pairs:
+        for s in range(ns):
+            for b in range(nclust):
+                c1, c2 = wctb[s, r1, b], wctb[s, r2, b]
+                before = int(E0[s, r1, c1]) + int(E0[s, r2, c2])
+                after = int(E1[s, r1, c1]) + int(E1[s, r2, c2])
+                bad += before != after
+                moved[s, r1, c1] = moved[s, r2, c2] = True
+    assert np.array_equal(E0[~moved], E1[~moved]), "an energy outside the moved pairs changed"
+    assert not np.array_equal(E0, E1), "no cluster flipped"
+    assert bad == 0, "%d pair sums changed" % bad
+    job.close()
+
+
+def test_cluster_exact_rule_bin_matches_oracle():
+    """EA_CLUSTER_EXACT at L = 24 (where it differs from the reference rule):
+    a whole bin with cluster moves equals the oracle run with the exact rule."""
+    betas, cum = lut("T07_16_N8")
+    job = eagb.new_job(24, 16, betas, cum, nsamples=3, bc=O.OBC, masters=MASTERS, iter0=0, jobid=6)
+    eagb._ck(eagb.lib().ea_set_cluster_rule(job.ctx, 1))
+    sim = O.Sim(24, 16, betas, cum, nbits=3, bc=O.OBC, masters=MASTERS, itmax=3)
+    it = 0
+    for _ in range(2):
+        avg, hist = job.run_bin(itmax=3, houfr=2, mesfr=1, ptfr=1, cluster=True)
+        it = sim.run_bin(itmax=3, houfr=2, mesfr=1, ptfr=1, iter0=it, jobid=6, cluster_exact=True)
+        assert np.array_equal(avg, sim.avgE)
+        assert np.array_equal(hist, sim.hist)
+    assert_same_state(job, sim)
+    job.close()
+
+
+def test_headline_bin_31_samples():
+    """The timed configuration itself: L=24, Lz=192, OBC, NB=32 (T in
+    [0.6, 1.6]), NR=8, 31 samples -- every (sample, clone) stride of the
+    sweep tile and the cluster kernels at full size, the generator on its SM
+    partition -- one step of the timed cadence (5 x (sweep, energy, PT), one
+    Houdayer move, the energy measurement) against the oracle."""
+    betas, cum = lut("T06_16_N32")
+    job = eagb.new_job(24, 192, betas, cum, nsamples=31, bc=O.OBC, masters=MASTERS, iter0=0, jobid=0)
+    sim = O.Sim(24, 192, betas, cum, nbits=31, bc=O.OBC, masters=MASTERS, itmax=1)
+    avg, hist = job.run_bin(itmax=1, houfr=5, mesfr=1, ptfr=1, cluster=True)
+    assert job.rng_sms() == 32
+    sim.run_bin(itmax=1, houfr=5, mesfr=1, ptfr=1, iter0=0, jobid=0)
+    assert np.array_equal(avg, sim.avgE)
+    assert np.array_equal(hist, sim.hist)
+    assert_same_state(job, sim)
+    acc, att, raw = job.get_pt_stats()
+    assert np.array_equal(raw, sim.accraw) and np.array_equal(acc, sim.acc)
     job.close()
 
 
