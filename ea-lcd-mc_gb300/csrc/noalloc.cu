@@ -1,15 +1,18 @@
 // noalloc.cu -- energy measurement that allocates no device memory.
 //
-// Some callers cannot call cudaMalloc: code that records its work into a CUDA
-// graph while a stream capture is active (cudaMalloc is not allowed during
-// capture), host frameworks that own every device byte through their own pool,
-// and latency-critical loops that must not take the implicit device
-// synchronisation of an allocation.  ea_measure_energy_noalloc serves them: it
+// Some callers cannot call cudaMalloc: host frameworks that own every device
+// byte through their own pool (an allocation behind their back breaks their
+// accounting, and fails outright when the pool already holds the memory), and
+// latency-critical loops that must not take the device-wide synchronisation
+// an allocation may imply.  ea_measure_energy_noalloc serves them: it
 // computes the same energies as ea_measure_energy for spins and couplings that
 // the caller already keeps in device memory, and writes them to a caller
 // buffer.  Its scratch space -- the per-tile partial sums of the energy kernel
 // and the neighbour tables of the geometry -- is the file-scope array below,
 // which every GPU that loads libeagb.so holds until the process exits.
+#include <cuda.h>
+
+#include <cstdio>
 #include <cstring>
 #include <mutex>
 
@@ -33,7 +36,29 @@ static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
+// Device address of g_scratch per device, with the context it was looked up
+// in: a recreated context (cudaDeviceReset) reloads the module, and the
+// array may then sit at another address.
 void *g_addr[kMaxDevices] = {};
+CUcontext g_ctx[kMaxDevices] = {};
+
+// The calling thread's current context (driver entry point looked up at run
+// time; the library does not link the driver library).  nullptr if the
+// lookup fails, which keeps one address per device.
+CUcontext current_context() {
+  using GetCurrent = CUresult (*)(CUcontext *);
+  static GetCurrent fn = []() -> GetCurrent {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, CUDA_VERSION, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return nullptr;
+    return reinterpret_cast<GetCurrent>(f);
+  }();
+  CUcontext c = nullptr;
+  if (!fn || fn(&c) != CUDA_SUCCESS) return nullptr;
+  return c;
+}
 
 // Neighbour half indices and flags of the multispin lattice, written into the
 // scratch tables (same tables as the context builds on the host: wrap-around
@@ -91,18 +116,31 @@ extern "C" int ea_measure_energy_noalloc(const ea_geom *gp, const uint64_t *d_sp
     set_last_error("ea_measure_energy_noalloc: no current CUDA device");
     return EA_ERR_CUDA;
   }
+  // an error left by the caller's own earlier work is theirs: report it and
+  // leave it pending instead of taking it for a failure of the launches below
+  const cudaError_t pending = cudaPeekAtLastError();
+  if (pending != cudaSuccess) {
+    char msg[256];
+    std::snprintf(msg, sizeof(msg), "ea_measure_energy_noalloc: a CUDA error is pending from earlier work: %s",
+                  cudaGetErrorString(pending));
+    set_last_error(msg);
+    return EA_ERR_CUDA;
+  }
   unsigned char *base;
   {
-    // once per device, with that device current: the device address of the
-    // scratch array (the host-side name g_scratch is not a device address)
+    // once per device (and again if its context was recreated), with that
+    // device current: the device address of the scratch array (the host-side
+    // name g_scratch is not a device address)
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_addr[dev]) {
+    const CUcontext ctx = current_context();
+    if (!g_addr[dev] || g_ctx[dev] != ctx) {
       void *p = nullptr;
       if (cudaGetSymbolAddress(&p, g_scratch) != cudaSuccess || !p) {
         set_last_error("ea_measure_energy_noalloc: cudaGetSymbolAddress of the scratch array failed");
         return EA_ERR_CUDA;
       }
       g_addr[dev] = p;
+      g_ctx[dev] = ctx;
     }
     base = static_cast<unsigned char *>(g_addr[dev]);
   }
@@ -118,10 +156,18 @@ extern "C" int ea_measure_energy_noalloc(const ea_geom *gp, const uint64_t *d_sp
   j.nbidx = reinterpret_cast<const int32_t *>(base + kPartBytes);
   j.nbflag = base + kPartBytes + kIdxBytes;
   j.E = d_energies;
+  // each launch checked right after it is made
+  const char *failed = nullptr;
+  cudaError_t e;
   k_noalloc_tables<<<(g.msc_v + 255) / 256, 256, 0, st>>>(g.msc_l, g.msc_lz, g.half);
-  if (cudaGetLastError() != cudaSuccess || launch_energy(j, st) != cudaSuccess ||
-      launch_energy_reduce(j, st) != cudaSuccess) {
-    set_last_error("ea_measure_energy_noalloc: kernel launch failed");
+  if ((e = cudaGetLastError()) != cudaSuccess) failed = "neighbour tables";
+  else if ((e = launch_energy(j, st)) != cudaSuccess) failed = "energy partial sums";
+  else if ((e = launch_energy_reduce(j, st)) != cudaSuccess) failed = "energy reduction";
+  if (failed) {
+    char msg[256];
+    std::snprintf(msg, sizeof(msg), "ea_measure_energy_noalloc: launch of the %s kernel failed: %s", failed,
+                  cudaGetErrorString(e));
+    set_last_error(msg);
     return EA_ERR_CUDA;
   }
   return EA_OK;
