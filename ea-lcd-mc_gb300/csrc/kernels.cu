@@ -241,9 +241,8 @@ cudaError_t launch_houdayer_pairs(const JobDev &j, cudaStream_t st) {
 }
 
 cudaError_t launch_houdayer_group(const JobDev &j, int g, cudaStream_t st) {
-  const size_t nw = (size_t)j.ns * j.nclust * 2 * j.half;
   const size_t ns = (size_t)j.ns * j.nclust * j.V;
-  const unsigned bw = (unsigned)((nw + 255) / 256), bs = (unsigned)((ns + 255) / 256);
+  const unsigned bs = (unsigned)((ns + 255) / 256);
   const unsigned nlat = (unsigned)(j.ns * j.nclust);
   k_hou_overlap<<<dim3((2 * j.half + 255) / 256, nlat), 256, 0, st>>>(j, g);
   int D, P, nslab;

@@ -2,7 +2,8 @@
 """Generate host-side golden fixtures from the reference's own code.
 
 Runs only where the reference tree is present (it reads the reference sources
-at /root/reference/PROGRAM through oracle/Makefile).  For each geometry below
+in the folder EA_REF names, the reference's PROGRAM folder, through
+oracle/Makefile).  For each geometry below
 it compiles the reference host code (random_generator.cu, ini.c, io.c, upd.c,
 med.c) with oracle/ref_host_harness.cpp, runs it with fixed master seeds and
 stores what it computed in tests/golden/host_<TAG>.npz.  It also compiles the
@@ -24,7 +25,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 ORACLE = os.path.join(ROOT, "oracle")
-REF = os.environ.get("EA_REF", "/root/reference/PROGRAM")
+# EA_REF: the reference's PROGRAM folder (required where the reference is read)
+REF = os.environ.get("EA_REF", "")
 
 MASTERS = (81985529216486895, 1147797409030816545, 1229782938247303441, 6148914691236517205)
 
@@ -86,7 +88,7 @@ def lut_fixture(name, betas, work):
         bfile = os.path.join(REF, "input", "betas_T07_T20_N40")
     else:
         write_betas(bfile, betas)
-    subprocess.run(["make", "-s", "-C", ORACLE, "ref-lut", "CFG=8,8,%d,PBC" % nb], check=True)
+    subprocess.run(["make", "-s", "-C", ORACLE, "ref-lut", "CFG=8,8,%d,PBC" % nb, "REF=" + REF], check=True)
     exe = os.path.join(ORACLE, "_ref", "create_LUT_NB%d" % nb)
     res = subprocess.run([exe, bfile], cwd=work, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE)
     refused = res.returncode != 0
@@ -120,8 +122,8 @@ def lut_fixture(name, betas, work):
 
 
 def main():
-    if not os.path.isdir(REF):
-        sys.exit("reference tree not found at %s" % REF)
+    if not REF or not os.path.isdir(REF):
+        sys.exit("set EA_REF to the reference's PROGRAM folder")
     work = tempfile.mkdtemp(prefix="eagold_")
     if sys.argv[1:] == ["luts"]:
         for name in EXTRA_LUTS:
@@ -132,7 +134,7 @@ def main():
         if bset not in done_luts:
             done_luts[bset] = lut_fixture(bset, beta_set(bset), work)
         betas = done_luts[bset]
-        subprocess.run(["make", "-s", "-C", ORACLE, "ref-host", "CFG=%d,%d,%d,%s" % (L, Lz, NB, BC)], check=True)
+        subprocess.run(["make", "-s", "-C", ORACLE, "ref-host", "CFG=%d,%d,%d,%s" % (L, Lz, NB, BC), "REF=" + REF], check=True)
         exe = os.path.join(ORACLE, "_ref", "host_" + tag, "harness")
         rundir = os.path.join(work, tag)
         os.makedirs(rundir, exist_ok=True)

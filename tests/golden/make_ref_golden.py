@@ -33,8 +33,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 ORACLE = os.path.join(ROOT, "oracle")
 RUNS = os.path.join(ORACLE, "_ref", "runs")
-REF = os.environ.get("EA_REF", "/root/reference/PROGRAM")
-OUT = os.environ.get("EA_REFGOLD_OUT", os.path.join("gpurun_out", "refgold"))
+# EA_REF: the reference's PROGRAM folder (required where the reference is read)
+REF = os.environ.get("EA_REF", "")
+# EA_REFGOLD_OUT: folder, relative to the repository root, that the GPU host
+# hands back with the reference outputs (required by stage and collect)
+OUT = os.environ.get("EA_REFGOLD_OUT", "")
 MASTERS = (81985529216486895, 1147797409030816545, 1229782938247303441, 6148914691236517205)
 
 # tag: L, Lz, BC, cluster, lut-set, isample, nbits, list_samples, nbin, itmax, houfr, mesfr, ptfr, resume_nbin
@@ -67,10 +70,12 @@ def case_inputs(tag, dirpath):
 
 
 def stage():
-    if not os.path.isdir(REF):
-        sys.exit("reference tree not found")
+    if not REF or not os.path.isdir(REF):
+        sys.exit("set EA_REF to the reference's PROGRAM folder")
+    if not OUT:
+        sys.exit("set EA_REFGOLD_OUT to the folder the GPU host hands back")
     shutil.rmtree(RUNS, ignore_errors=True)
-    subprocess.run(["make", "-s", "-C", ORACLE, "ref-stage"], check=True)
+    subprocess.run(["make", "-s", "-C", ORACLE, "ref-stage", "REF=" + REF], check=True)
     lines = ["#!/bin/bash", "# builds and runs the reference binary for every golden case (GPU host)",
              "set -u", "cd \"$(dirname \"$0\")/../../..\"", "R=$PWD", "mkdir -p %s" % OUT,
              "nvidia-smi -L > %s/gpu.txt 2>&1" % OUT, "builds=()"]
@@ -97,6 +102,8 @@ def stage():
 
 
 def collect():
+    if not OUT:
+        sys.exit("set EA_REFGOLD_OUT to the folder the GPU host handed back")
     src = os.path.join(ROOT, OUT)
     for tag in CASES:
         base = os.path.join(src, tag)
