@@ -31,9 +31,15 @@ L, LZ, NR, NS, HOUFR = 24, 192, 8, 31, 5
 LUT = os.path.join(ROOT, "tests", "golden", "lut_T06_16_N32.npz")
 MASTERS = (0x1234567890ABCDEF, 0x0FEDCBA987654321, 0x1111222233334444, 0x5555666677778888)
 WORKLOAD = "L24_Lz192_OBC_NB32_NR8_ns31_ptfr1_houfr5"
-# DRAM bytes (read + write) of one k_sweep launch of this workload, from an
-# ncu capture (mean of two launches)
+# DRAM bytes (read + write) of one k_sweep launch of this workload, from the
+# ncu capture of the bench's k_sweep launches (mean of two launches)
 KSWEEP_DRAM_BYTES = 136.0e6
+# The integer-op model of the fused sweep (the Philox4x32-10 rounds, the
+# post-mix and rotation of a random word, the threshold search per byte, the
+# bit-sliced update per word), in 32-bit operations: 6 Philox calls of
+# 78 + 18 + 4 ops and 24 searches of 6 + 6 x (iterations) ops per random
+# triple, 60 ops per updated word.
+OPS_TRIPLE_BASE, OPS_PER_ITER, OPS_WORD = 6 * (78 + 18 + 4) + 24 * 6, 24 * 6, 60
 # mixed-geometry workload of the batched vs plain comparison: every
 # L x (Lz/L) x boundary x NT combination is one job class
 # (36 geometry classes; either 36 jobs of 32 samples or 288 jobs of 4)
@@ -55,6 +61,69 @@ def peaks():
         return float(d["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+def lut_search_iters(cum):
+    """Expected iterations of the threshold search of one byte for a uniform
+    64-bit R: the bisection between the bounds of the 8-bit pre-search
+    (lut_byte in kernels_dev.cuh), weighted by the exact probability of each
+    result byte within each of the 256 pre-search buckets."""
+    c = [int(x) for x in np.asarray(cum, np.uint64)]
+
+    def first_above(R):
+        n = 0
+        while n < 255 and not R < c[n]:
+            n += 1
+        return n
+
+    tot = 0
+    for t in range(256):
+        lo_r, hi_r = t << 56, ((t + 1) << 56) - 1
+        a0, b0 = first_above(lo_r), first_above(hi_r)
+        for n in range(a0, b0 + 1):
+            lo = max(c[n - 1] if n > 0 else 0, lo_r)
+            hi = hi_r if n == 255 else min(c[n] - 1, hi_r)
+            if hi < lo:
+                continue
+            a, b, d = a0, b0, 0
+            while a < b:
+                m = (a + b) >> 1
+                d += 1
+                if n <= m:
+                    b = m
+                else:
+                    a = m + 1
+            tot += (hi - lo + 1) * d
+    return tot / float(1 << 64)
+
+
+def int_ops(cums, triples, words):
+    """32-bit integer operations of a launch that draws `triples` random
+    triples (spread evenly over the temperatures of `cums`) and updates
+    `words` spin words."""
+    e = float(np.mean([lut_search_iters(c) for c in cums]))
+    return triples * (OPS_TRIPLE_BASE + OPS_PER_ITER * e) + words * OPS_WORD, e
+
+
+_int_peak = None
+
+
+def int_peak(eagb, dev):
+    """Measured 32-bit integer instruction rate of this GPU (ops/s, all SMs)."""
+    global _int_peak
+    if _int_peak is None:
+        alu, imad = C.c_double(), C.c_double()
+        eagb._ck(eagb.lib().ea_probe_int32_rate(dev, C.byref(alu), C.byref(imad)))
+        _int_peak = (alu.value, imad.value)
+    return _int_peak
+
+
+def headline_config():
+    """The workload of the headline line, the same for both arms."""
+    return {"workload": WORKLOAD, "L": L, "Lz": LZ, "nbetas": 32, "nrep": NR, "nsamples": NS, "bc": "OBC",
+            "ptfr": 1, "houfr": HOUFR, "cluster": "Houdayer move on the colder half every 5 sweeps",
+            "step": "5 x (sweep + energy + parallel tempering) + 1 Houdayer move + energy measurement",
+            "l2": "flushed between steps (512 MB write)"}
 
 
 class Clocks:
@@ -105,43 +174,43 @@ class Clocks:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_sample(nthreads, sweeps=1):
-    """Reference algorithm (oracle C restatement) on host cores: one sample of the
-    bench geometry, `sweeps` Metropolis sweeps.  Returns (spin updates, seconds)."""
+def cpu_cycle(nsteps, warmup=0):
+    """The reference algorithm on the host cores (the oracle's C restatement,
+    OpenMP over every core): the headline workload itself -- 31 samples, the
+    same cadence as one GPU step (5 x (sweep + energy + FP64 parallel
+    tempering) + a Houdayer move with the host cuRAND generator + the energy
+    measurement) -- for `warmup` untimed and `nsteps` timed steps.  Returns
+    (spin updates, seconds) of the timed steps."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_py as O
     d = np.load(LUT)
-    sim = O.Sim(L, LZ, d["betas"], d["cum"], nbits=1, NR=NR, bc=O.OBC, masters=MASTERS)
-    t0 = time.perf_counter()
-    it = 0
-    for _ in range(sweeps):
-        for p in (0, 1):
-            ctr = O.fill_bits(sim.prc, sim.xo, NR, it, 0)
-            sim.half_sweep(ctr, p, nthreads)
-            it += 1
-    dt = time.perf_counter() - t0
-    return L * L * LZ * NR * len(d["betas"]) * sweeps, dt
+    sim = O.Sim(L, LZ, d["betas"], d["cum"], nbits=NS, NR=NR, bc=O.OBC, masters=MASTERS, itmax=1)
+    it, dt = 0, 0.0
+    for i in range(warmup + nsteps):
+        t0 = time.perf_counter()
+        it = sim.run_bin(itmax=1, houfr=HOUFR, mesfr=1, ptfr=1, iter0=it, jobid=0, cluster=True)
+        if i >= warmup:
+            dt += time.perf_counter() - t0
+    return HOUFR * L * L * LZ * NR * len(d["betas"]) * NS * nsteps, dt
+
+
+CPU_SAMPLE = ("31 samples x the full step of the GPU arm (5 sweeps with energy and FP64 tempering, a Houdayer "
+              "move with host cuRAND uniforms, the energy measurement), oracle C restatement, OpenMP")
 
 
 def run_reference(args, rank, world):
     if rank != 0:
         return
     n = os.cpu_count() or 1
-    vals = []
-    for i in range(args.warmup + args.steps):
-        su, dt = cpu_sample(n)
-        if i >= args.warmup:
-            vals.append((su, dt))
-    su = sum(v[0] for v in vals)
-    dt = sum(v[1] for v in vals)
+    su, dt = cpu_cycle(args.steps, args.warmup)
     value = su / dt / 1e12
     line = {"metric": "spin_updates_per_ps", "value": value, "unit": "spin-updates/ps", "impl": "reference",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
             "data": "synthetic (seeded couplings and spins as the reference generates them)",
-            "config": {"workload": WORKLOAD, "sample": "1 disorder sample x 1 sweep per step"},
+            "config": headline_config(),
             "cpu_baseline": {"value": value, "unit": "spin-updates/ps", "cores": n, "kind": "port",
-                             "sample": "1 sample x 1 Metropolis sweep of L24 Lz192 NB32 NR8 per step, oracle C restatement, OpenMP"},
+                             "sample": CPU_SAMPLE + "; every step of the run"},
             "e2e": {"value": value, "unit": "spin-updates/ps", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -600,30 +669,62 @@ def run_ours(args, rank, world, local):
     value = world * su_step * args.steps / (ms * 1e-3) / 1e12
     e2e = world * su_step * ne / e2e_s / 1e12
     hbm, how = peaks()
-    # algorithmic bytes of one half-sweep launch: read + write every word of the
-    # updated parity, read every word of the other parity once, read the couplings
+    ipk_alu, ipk_imad = int_peak(eagb, dev)
+    # k_sweep (one half-sweep launch): algorithmic bytes = read + write every
+    # word of the updated parity, read every word of the other parity once,
+    # read the couplings; algorithmic integer ops = the random triples of the
+    # launch (one per temperature, half-site and replica, shared by the 31
+    # samples) and the word updates
     words_parity = NS * NB * half * NR
     alg_bytes = words_parity * 8 * 3 + NS * 6 * half * 8
     sweep_ms = sw_ms.value / max(1, nsw.value)
     achieved = alg_bytes / (sweep_ms * 1e-3) / 1e9
+    ops, e_iters = int_ops(cum, NB * half * NR, words_parity)
+    int_achieved = ops / (sweep_ms * 1e-3)
+    hbm_frac, int_frac = achieved / hbm, int_achieved / ipk_alu
+    # the cluster labelling group of a move (overlap words, slab labelling,
+    # face merge, compression, selection + flip), per lattice site of the
+    # nclust = 16 colder temperatures, 31 samples and 2 replica groups:
+    # 3/8 B of overlap bits (two replicas read, one word written), 4 B label
+    # written, 4 B label read at the flip, 8 B uniform of the site's cluster
+    # (counted for every site: the generator draws one per site), and the two
+    # replicas' spin bits read and written (1/2 B)
+    nclust = 16
+    cl_sites = V * nclust * NS * 2
+    cl_bytes_site = 3.0 / 8 + 4 + 4 + 8 + 0.5
+    cl_move_ms = cl_ms.value / max(1, args.steps)
+    cl_achieved = cl_sites * cl_bytes_site / (cl_move_ms * 1e-3) / 1e9
+    roof = {"bound": "int32" if int_frac > hbm_frac else "hbm",
+            "achieved": int_achieved / 1e9 if int_frac > hbm_frac else achieved,
+            "peak": ipk_alu / 1e9 if int_frac > hbm_frac else hbm,
+            "unit": "Gop/s" if int_frac > hbm_frac else "GB/s",
+            "frac": max(hbm_frac, int_frac), "traffic": KSWEEP_DRAM_BYTES,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per k_sweep launch of this workload",
+            "kernel": "k_sweep", "peak_kind": how, "launch_ms": sweep_ms, "launches": nsw.value,
+            "hbm_frac": hbm_frac, "hbm_achieved_gbs": achieved, "hbm_peak_gbs": hbm, "alg_bytes_per_launch": alg_bytes,
+            "int_frac": int_frac, "int_achieved_gops": int_achieved / 1e9, "int_peak_gops": ipk_alu / 1e9,
+            "int_peak_source": "measured at the start of this run: independent 32-bit xor/add instruction chains "
+                               "on all SMs (ea_probe_int32_rate); multiply-add chains ran at %.0f Gop/s"
+                               % (ipk_imad / 1e9),
+            "int_ops_per_launch": ops, "int_ops_per_spin_update": ops / (64.0 * words_parity),
+            "search_iterations_per_byte": e_iters,
+            "cluster": {"kernels": "k_overlap, k_cc_slab, k_cc_merge, k_cc_compress, k_flip (one move, 2 groups)",
+                        "bound": "hbm", "alg_bytes_per_site": cl_bytes_site, "sites_per_move": cl_sites,
+                        "move_ms": cl_move_ms, "achieved": cl_achieved, "peak": hbm, "unit": "GB/s",
+                        "frac": cl_achieved / hbm, "site_labellings_per_ns": cl_sites / (cl_move_ms * 1e6),
+                        "note": "labelling is bound by instruction issue and SMEM latency, not DRAM"}}
     line = {
         "metric": "spin_updates_per_ps", "value": value, "unit": "spin-updates/ps", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u64",
         "data": "synthetic (seeded couplings and spins as the reference generates them)",
-        "config": {"workload": WORKLOAD, "L": L, "Lz": LZ, "nbetas": NB, "nrep": NR, "nsamples": NS,
-                   "bc": "OBC", "ptfr": 1, "houfr": HOUFR, "form": "plain (one job per launch)",
-                   "l2": "flushed between steps (512 MB write)", "parallelism": "replicas" if world > 1 else "single",
-                   "rng_sms": job.rng_sms()},
+        "config": headline_config(),
+        "form": "plain (one job per launch)", "parallelism": "replicas" if world > 1 else "single",
+        "rng_sms": job.rng_sms(),
         "e2e": {"value": e2e, "unit": "spin-updates/ps", "h2d_bytes_per_step": NS * 2 * nw * 8,
                 "d2h_bytes_per_step": NS * NR * NB * 4},
         "gpu_launches": args.steps * (HOUFR * 6 + 1 + 2 * 4 + 3),
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": KSWEEP_DRAM_BYTES, "traffic_source": "ncu dram__bytes_read+write per k_sweep launch "
-                     "of this workload (profiles/k_sweep_dram_bench_L24_Lz192_NB32_ns31.md)",
-                     "kernel": "k_sweep", "peak_kind": how,
-                     "binding_pipe": "integer ALU: 58.4 % of peak in ncu (profiles/k_sweep_full_bench_L24_Lz192_NB32_ns31.md)",
-                     "alg_bytes_per_launch": alg_bytes, "launch_ms": sweep_ms, "launches": nsw.value},
+        "roofline": roof,
         "kernel_ms": {"sweep": sw_ms.value, "pt": pt_ms.value, "cluster": cl_ms.value,
                       "uniforms_overlapped": rg_ms.value, "step_total": ms},
         "clocks": clk.summary(),
@@ -637,9 +738,9 @@ def run_ours(args, rank, world, local):
     if not args.no_sp:
         line["sample_packed"] = run_sp(args, dev, torch, eagb)
     if not args.no_cpu:
-        su, dt = cpu_sample(os.cpu_count() or 1, sweeps=20)
+        su, dt = cpu_cycle(2)
         line["cpu_baseline"] = {"value": su / dt / 1e12, "unit": "spin-updates/ps", "cores": os.cpu_count(),
-                                "kind": "port", "sample": "1 sample x 1 Metropolis sweep of the same geometry"}
+                                "kind": "port", "sample": CPU_SAMPLE + "; 2 steps"}
     print(json.dumps(line), flush=True)
     job.close()
 
