@@ -174,10 +174,10 @@ int sp_energy_chunk(const SpDev &d) {
   return c < 16 ? 16 : (c > kSpChunkMax ? kSpChunkMax : c);
 }
 
-__device__ __forceinline__ void sp_energy_body(const SpDev &d, int blk) {
+// col: the thread's index over nw * nchunk * G (blocks of 256 threads).
+__device__ __forceinline__ void sp_energy_body(const SpDev &d, long long col) {
   const int G = d.NR * d.NB, V = d.V, chunk = d.echunk;
   const int nchunk = (V + chunk - 1) / chunk;
-  const long long col = (long long)blk * blockDim.x + threadIdx.x;  // over nw * nchunk * G
   if (col >= (long long)d.nw * nchunk * G) return;
   const int rb = (int)(col % G), ch = (int)((col / G) % nchunk), w = (int)(col / ((long long)G * nchunk));
   const u64 *Sw = d.S + (size_t)w * V * G + rb;
@@ -234,9 +234,10 @@ __device__ __forceinline__ void sp_energy_body(const SpDev &d, int blk) {
 // draw replaces the 2 KB of state per chain.  A warp holds 32 samples of one
 // (word, replica): the accepted swaps of pair i form the lane mask M[i].
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void sp_pt_body(const SpDev &d, int wr) {
+// wr = (word, replica); lane = sample, 0..63, the 64 lanes two whole warps.
+__device__ __forceinline__ void sp_pt_body(const SpDev &d, int wr, int lane) {
   const int NB = d.NB, NR = d.NR, G = NR * NB;
-  const int w = wr / NR, r = wr % NR, lane = threadIdx.x;
+  const int w = wr / NR, r = wr % NR;
   const int nt = 3 * d.V;
   const size_t o = ((size_t)w * 64 + lane) * G + (size_t)r * NB;
   const unsigned long long step = *d.ptstep;
@@ -684,11 +685,11 @@ __global__ void kb_sp_zero(const __grid_constant__ SpBatchDev b) {
 }
 __global__ void __launch_bounds__(256) kb_sp_energy(const __grid_constant__ SpBatchDev b) {
   SPB_ITEM(SPB_ENERGY)
-  sp_energy_body(d, blk);
+  sp_energy_body(d, (long long)blk * blockDim.x + threadIdx.x);
 }
 __global__ void __launch_bounds__(64) kb_sp_pt(const __grid_constant__ SpBatchDev b) {
   SPB_ITEM(SPB_PT)
-  sp_pt_body(d, blk);
+  sp_pt_body(d, blk, threadIdx.x);
 }
 __global__ void __launch_bounds__(kPermRows) kb_sp_permute(const __grid_constant__ SpBatchDev b) {
   extern __shared__ u64 rows[];
@@ -795,6 +796,188 @@ cudaError_t sp_batch_measure(const SpBatchDev &b, cudaStream_t st) {
 }
 
 // ---------------------------------------------------------------------------
+// Persistent bin kernel: one cooperative launch runs whole bins of a set of
+// jobs (one job, or a batch), every phase of the cadence -- colour passes
+// with their counters, energies, tempering, permutes, Houdayer moves,
+// measurements -- as a loop over the same packed (job, block) work list the
+// batched kernels use, with a grid barrier between phases.  The bodies are
+// the one-job kernels', in the same order, so the words are the same as with
+// one launch per phase; what goes away is the launch and graph-node gap of
+// every phase, which bounds jobs too small to fill the GPU.
+// ---------------------------------------------------------------------------
+constexpr int kPersistThreads = 512;
+constexpr unsigned long long kBarrierWaitNs = 4000000000ull;  // 4 s
+
+__device__ __forceinline__ unsigned long long sp_globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Grid barrier of a cooperative launch (every block resident): arrivals are
+// counted in *bar (zero at launch); the k-th barrier of the launch waits for
+// k x gridDim.x arrivals.  A wait gives up after kBarrierWaitNs, or as soon
+// as another block has given up, counts that in *err and returns false; the
+// kernel then returns, so no block waits for ever and the host reports the
+// failure.
+__device__ bool sp_grid_sync(const SpPersistDev &p, unsigned &epoch) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ++epoch;
+    const unsigned long long target = (unsigned long long)epoch * gridDim.x;
+    __threadfence();
+    atomicAdd(p.bar, 1ull);
+    int ok = 1;
+    const unsigned long long t0 = sp_globaltimer();
+    for (;;) {
+      unsigned long long v;
+      asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p.bar) : "memory");
+      if (v >= target) break;
+      if (*(volatile int *)p.err) { ok = 0; break; }
+      if (sp_globaltimer() - t0 > kBarrierWaitNs) { atomicAdd(p.err, 1); ok = 0; break; }
+      __nanosleep(64);
+    }
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// The blocks of one work-list kind whose bodies need a whole thread block.
+#define SPP_BLOCKS(KIND, BODY)                                                        \
+  for (uint32_t vb = blockIdx.x; vb < b.total[KIND]; vb += gridDim.x) {              \
+    __syncthreads();                                                                  \
+    if (threadIdx.x == 0) {                                                           \
+      const int jb_ = spb_job(b.pre[KIND], b.njobs, vb);                              \
+      s_job[0] = b.jobs[jb_];                                                         \
+      s_blk[0] = (int)(vb - __ldg(b.pre[KIND] + jb_));                                \
+    }                                                                                 \
+    __syncthreads();                                                                  \
+    const SpDev &d = s_job[0];                                                        \
+    const int blk = s_blk[0];                                                         \
+    BODY;                                                                             \
+  }
+
+// Kinds whose one-job blocks have SUB threads and no barrier: each thread
+// block takes kPersistThreads / SUB of them at a time.
+#define SPP_SUB(KIND, SUB, BODY)                                                      \
+  for (uint32_t vb0 = blockIdx.x * (kPersistThreads / SUB); vb0 < b.total[KIND];      \
+       vb0 += gridDim.x * (kPersistThreads / SUB)) {                                 \
+    const int sub = threadIdx.x / SUB, ltid = threadIdx.x % SUB;                      \
+    const uint32_t vb = vb0 + sub;                                                    \
+    __syncthreads();                                                                  \
+    if (ltid == 0 && vb < b.total[KIND]) {                                            \
+      const int jb_ = spb_job(b.pre[KIND], b.njobs, vb);                              \
+      s_job[sub] = b.jobs[jb_];                                                       \
+      s_blk[sub] = (int)(vb - __ldg(b.pre[KIND] + jb_));                              \
+    }                                                                                 \
+    __syncthreads();                                                                  \
+    if (vb < b.total[KIND]) {                                                         \
+      const SpDev &d = s_job[sub];                                                    \
+      const int blk = s_blk[sub];                                                     \
+      BODY;                                                                           \
+    }                                                                                 \
+  }
+
+#define SPP_SYNC() \
+  if (!sp_grid_sync(p, epoch)) return
+
+__global__ void __launch_bounds__(kPersistThreads, 1) k_sp_persist(const __grid_constant__ SpPersistDev p) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ SpDev s_job[kPersistThreads / 64];
+  __shared__ int s_blk[kPersistThreads / 64];
+  const SpBatchDev &b = p.b;
+  unsigned epoch = 0;
+  auto energy = [&]() -> bool {
+    SPP_SUB(SPB_ZERO, 256, {
+      const long long i = (long long)blk * 256 + ltid;
+      if (i < (long long)d.nw * 64 * d.NR * d.NB) d.U2[i] = 0;
+    })
+    if (!sp_grid_sync(p, epoch)) return false;
+    SPP_SUB(SPB_ENERGY, 256, sp_energy_body(d, (long long)blk * 256 + ltid))
+    return sp_grid_sync(p, epoch);
+  };
+  for (int it = 0; it < p.itmax; ++it) {
+    for (int im = 0; im < p.mesfr; ++im) {
+      for (int ih = 0; ih < p.houfr; ++ih) {
+        for (int sw = 0; sw < p.ptfr; ++sw) {
+          for (int c = 0; c < p.ncol_max; ++c) {
+            for (int j = blockIdx.x; j < b.njobs; j += gridDim.x) {
+              __syncthreads();
+              if (threadIdx.x == 0) s_job[0] = b.jobs[j];
+              __syncthreads();
+              if (c < s_job[0].ncol) sp_fill_body(s_job[0]);
+            }
+            SPP_SYNC();
+            SPP_BLOCKS(SPB_PASS0 + c, sp_pass_body(d, d.col_off[c], d.col_off[c + 1] - d.col_off[c], blk, smem))
+            SPP_SYNC();
+          }
+        }
+        if (!energy()) return;
+        SPP_SUB(SPB_PT, 64, sp_pt_body(d, blk, ltid))
+        SPP_SYNC();
+        SPP_BLOCKS(SPB_PERMUTE, sp_permute_body(d, blk, reinterpret_cast<u64 *>(smem)))
+        SPP_SYNC();
+      }
+      if (p.cluster) {
+        for (int j = blockIdx.x * kPersistThreads + threadIdx.x; j < b.njobs; j += gridDim.x * kPersistThreads)
+          if (b.jobs[j].nclust > 0) sp_pairs_body(b.jobs[j]);
+        SPP_SYNC();
+        for (int g = 0; g < 2; ++g) {
+          if (!b.total[SPB_CL0 + g]) continue;
+          SPP_SUB(SPB_OVL0 + g, 256, sp_overlap_body(d, g, (long long)blk * 256 + ltid))
+          SPP_SYNC();
+          SPP_BLOCKS(SPB_CL0 + g, {
+            if (d.V <= kSpCluster4MaxV) sp_cluster4_body(d, g, blk, reinterpret_cast<uint32_t *>(smem));
+            else sp_cluster_body(d, g, blk, reinterpret_cast<uint32_t *>(smem));
+          })
+          SPP_SYNC();
+          SPP_SUB(SPB_FL0 + g, 256, sp_flip_body(d, g, (long long)blk * 256 + ltid))
+          SPP_SYNC();
+        }
+      }
+    }
+    if (!energy()) return;
+    SPP_SUB(SPB_MEASURE, 256, sp_measure_u2_body(d, (long long)blk * 256 + ltid))
+    SPP_SYNC();
+  }
+}
+
+#undef SPP_SYNC
+#undef SPP_SUB
+#undef SPP_BLOCKS
+
+// Blocks of a cooperative launch of k_sp_persist with `smem` bytes of dynamic
+// SMEM: every block resident at once (one per SM, the kernel's registers and
+// SMEM allowing), and no more than the largest phase has work for.
+int sp_persist_grid(const SpBatchDev &b, size_t smem) {
+  int dev = 0, nsm = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return 0;
+  if (cudaFuncSetAttribute(k_sp_persist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sp_persist, kPersistThreads, smem) != cudaSuccess ||
+      per_sm < 1)
+    return 0;
+  uint32_t work = (uint32_t)b.njobs;
+  for (int k = 0; k < SPB_COUNT; ++k) {
+    const uint32_t sub = (k == SPB_PT) ? kPersistThreads / 64
+                         : (k >= SPB_PASS0 && k <= SPB_PASS3) || k == SPB_PERMUTE || k == SPB_CL0 || k == SPB_CL1
+                             ? 1 : kPersistThreads / 256;
+    work = std::max(work, (b.total[k] + sub - 1) / sub);
+  }
+  return (int)std::min<uint32_t>(work, (uint32_t)(per_sm * nsm));
+}
+
+cudaError_t sp_launch_persist(const SpPersistDev &p, int grid, size_t smem, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(p.bar, 0, sizeof(unsigned long long), st);
+  if (e != cudaSuccess) return e;
+  void *args[] = {const_cast<SpPersistDev *>(&p)};
+  return cudaLaunchCooperativeKernel((const void *)k_sp_persist, dim3(grid), dim3(kPersistThreads), args, smem, st);
+}
+
+// ---------------------------------------------------------------------------
 // One-job kernels: the bodies above, one block per item
 // ---------------------------------------------------------------------------
 __global__ void k_sp_fill(const __grid_constant__ SpDev d) { sp_fill_body(d); }
@@ -802,8 +985,10 @@ __global__ void __launch_bounds__(512) k_sp_pass(const __grid_constant__ SpDev d
   extern __shared__ __align__(16) unsigned char smem[];
   sp_pass_body(d, off, n, blockIdx.x, smem);
 }
-__global__ void __launch_bounds__(256) k_sp_energy(const __grid_constant__ SpDev d) { sp_energy_body(d, blockIdx.x); }
-__global__ void __launch_bounds__(64) k_sp_pt(const __grid_constant__ SpDev d) { sp_pt_body(d, blockIdx.x); }
+__global__ void __launch_bounds__(256) k_sp_energy(const __grid_constant__ SpDev d) {
+  sp_energy_body(d, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
+__global__ void __launch_bounds__(64) k_sp_pt(const __grid_constant__ SpDev d) { sp_pt_body(d, blockIdx.x, threadIdx.x); }
 __global__ void __launch_bounds__(kPermRows) k_sp_permute(const __grid_constant__ SpDev d) {
   extern __shared__ u64 rows[];
   sp_permute_body(d, blockIdx.x, rows);
@@ -973,6 +1158,14 @@ struct ea_sp {
   int q_cap = 0;  // slots the overlap buffer holds
   SpDev it_dev{};  // the descriptor the graph was captured with
   int last_itmax = 0;  // iterations of the last bin (alone or batched)
+  // persistent bin kernel of the job alone (EA_BIN_*)
+  int bin_mode = EA_BIN_AUTO;
+  SpDev *p_jobs = nullptr;            // [1] descriptor of the work list
+  uint32_t *p_pre = nullptr;          // [SPB_COUNT][2] block prefix sums
+  unsigned long long *p_bar = nullptr;
+  int *p_err = nullptr;
+  SpDev p_up{};                       // descriptor last uploaded
+  bool p_valid = false;
 };
 
 namespace {
@@ -1083,6 +1276,10 @@ int ea_sp_destroy(ea_sp *c) {
   if (c->d.Q) cudaFree(c->d.Q);
   if (c->d.cscratch) cudaFree(c->d.cscratch);
   if (c->it_graph) cudaGraphExecDestroy(c->it_graph);
+  if (c->p_jobs) cudaFree(c->p_jobs);
+  if (c->p_pre) cudaFree(c->p_pre);
+  if (c->p_bar) cudaFree(c->p_bar);
+  if (c->p_err) cudaFree(c->p_err);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
   return EA_OK;
@@ -1101,10 +1298,29 @@ int ea_sp_stream(ea_sp *c, void **stream) {
   return EA_OK;
 }
 
+// After a synchronisation: did a persistent bin kernel give up on a barrier?
+static int sp_check_persist(int *d_err, cudaStream_t st) {
+  if (!d_err) return EA_OK;
+  int err = 0;
+  SCU(cudaMemcpyAsync(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  SCU(cudaStreamSynchronize(st));
+  if (err) {
+    SCU(cudaMemsetAsync(d_err, 0, sizeof(int), st));
+    return spfail(EA_ERR_CUDA, "persistent bin kernel: a grid barrier wait gave up (%d blocks); the bin is incomplete", err);
+  }
+  return EA_OK;
+}
+
 int ea_sp_sync(ea_sp *c) {
   if (!c) return spfail(EA_ERR_ARG, "null job");
   SCU(cudaSetDevice(c->device));
   SCU(cudaStreamSynchronize(c->st));
+  return sp_check_persist(c->p_err, c->st);
+}
+
+int ea_sp_set_bin_kernel(ea_sp *c, int32_t mode) {
+  if (!c || mode < EA_BIN_AUTO || mode > EA_BIN_PERSISTENT) return spfail(EA_ERR_ARG, "bad bin-kernel mode");
+  c->bin_mode = mode;
   return EA_OK;
 }
 
@@ -1321,6 +1537,59 @@ int ea_sp_houdayer(ea_sp *c, int32_t nclust) {
   return sp_houdayer(c, nclust);
 }
 
+// Batches whose jobs all have at most this many spin words run their bins in
+// the persistent kernel under EA_BIN_AUTO.  A job alone takes the graph: each
+// phase of a small job is a latency-bound chain that a barrier does not
+// shorten, and the graph's per-phase kernels run at twice the persistent
+// kernel's occupancy (measured: 84 vs 106 us per sweep at L=6, Lz=24, NT=12).
+constexpr double kSpPersistMaxWords = 1048576.0;
+
+static bool sp_small(const SpDev &d) {
+  return (double)d.nw * d.V * d.NR * d.NB <= kSpPersistMaxWords && d.ncol <= kSpBatchMaxColours;
+}
+
+static bool sp_use_persist(int mode, const SpDev &) { return mode == EA_BIN_PERSISTENT; }
+
+// The work list of the job alone (its blocks of every kind, as a batch of
+// one), uploaded when the descriptor changed; then one cooperative launch.
+static int sp_run_persist(ea_sp *c, const ea_cadence *cad) {
+  const SpDev &d = c->d;
+  if (d.ncol > kSpBatchMaxColours) return spfail(EA_ERR_ARG, "the persistent bin kernel takes up to %d colours", kSpBatchMaxColours);
+  if (!c->p_jobs) {
+    SCU(cudaMalloc((void **)&c->p_jobs, sizeof(SpDev)));
+    SCU(cudaMalloc((void **)&c->p_pre, sizeof(uint32_t) * SPB_COUNT * 2));
+    SCU(cudaMalloc((void **)&c->p_bar, sizeof(unsigned long long)));
+    SCU(cudaMalloc((void **)&c->p_err, sizeof(int)));
+    SCU(cudaMemsetAsync(c->p_err, 0, sizeof(int), c->st));
+  }
+  uint32_t cnt[SPB_COUNT];
+  sp_batch_blocks(d, cad->cluster != 0, cnt);
+  if (!c->p_valid || std::memcmp(&c->p_up, &d, sizeof(SpDev))) {
+    std::vector<uint32_t> pre((size_t)SPB_COUNT * 2);
+    for (int k = 0; k < SPB_COUNT; ++k) { pre[2 * k] = 0; pre[2 * k + 1] = cnt[k]; }
+    SCU(cudaStreamSynchronize(c->st));
+    SCU(cudaMemcpy(c->p_jobs, &d, sizeof(SpDev), cudaMemcpyHostToDevice));
+    SCU(cudaMemcpy(c->p_pre, pre.data(), sizeof(uint32_t) * pre.size(), cudaMemcpyHostToDevice));
+    c->p_up = d;
+    c->p_valid = true;
+  }
+  SpPersistDev p{};
+  p.b.jobs = c->p_jobs;
+  p.b.njobs = 1;
+  for (int k = 0; k < SPB_COUNT; ++k) { p.b.pre[k] = c->p_pre + 2 * k; p.b.total[k] = cnt[k]; }
+  p.itmax = cad->itmax; p.houfr = cad->houfr; p.mesfr = cad->mesfr; p.ptfr = cad->ptfr;
+  p.cluster = cad->cluster != 0 && d.nclust > 0;
+  p.ncol_max = d.ncol;
+  p.bar = c->p_bar;
+  p.err = c->p_err;
+  size_t smem = std::max(sp_sweep_smem(d.NB, d.NR, d.kt), (size_t)kPermRows * (d.NB | 1) * 8);
+  if (p.cluster) smem = std::max(smem, sp_cluster_smem(d.V));
+  const int grid = sp_persist_grid(p.b, smem);
+  if (grid < 1) return spfail(EA_ERR_CUDA, "persistent bin kernel: no co-resident grid for %zu bytes of shared memory", smem);
+  SCU(sp_launch_persist(p, grid, smem, c->st));
+  return EA_OK;
+}
+
 int ea_sp_run(ea_sp *c, const ea_cadence *cad, double *avgE) {
   if (!c || !cad || cad->itmax < 1 || cad->houfr < 1 || cad->mesfr < 1 || cad->ptfr < 1)
     return spfail(EA_ERR_ARG, "bad cadence");
@@ -1331,6 +1600,12 @@ int ea_sp_run(ea_sp *c, const ea_cadence *cad, double *avgE) {
   SCU(cudaMemsetAsync(d.avgE, 0, n * 8, c->st));
   int rc, nclust = cad->nclust;
   if (cad->cluster && (rc = sp_cluster_prepare(c, nclust))) return rc;
+  if (sp_use_persist(c->bin_mode, d)) {
+    if ((rc = sp_run_persist(c, cad))) return rc;
+    c->last_itmax = cad->itmax;
+    if (avgE) return ea_sp_bin_results(c, avgE);
+    return EA_OK;
+  }
   // one iteration: every launch reads its counters (pass, tempering step,
   // move) from the device, so the captured graph replays each iteration
   auto iteration = [&]() -> int {
@@ -1380,6 +1655,8 @@ int ea_sp_bin_results(ea_sp *c, double *avgE) {
   std::vector<double> h(n);
   SCU(cudaMemcpyAsync(h.data(), d.avgE, n * 8, cudaMemcpyDeviceToHost, c->st));
   SCU(cudaStreamSynchronize(c->st));
+  const int rc = sp_check_persist(c->p_err, c->st);
+  if (rc) return rc;
   for (size_t i = 0; i < n; ++i) avgE[i] = h[i] / c->last_itmax;
   return EA_OK;
 }
@@ -1420,6 +1697,11 @@ struct ea_sp_batch {
   cudaGraphExec_t it_graph = nullptr;
   ea_cadence it_cad{};
   std::vector<SpBatchDev> it_bd;
+  // persistent bin kernel: every job in one work list
+  int bin_mode = EA_BIN_AUTO;
+  SpClass all;
+  unsigned long long *p_bar = nullptr;
+  int *p_err = nullptr;
 };
 
 constexpr int kSpBatchBranches = 256;
@@ -1513,6 +1795,13 @@ int ea_sp_batch_create(ea_sp *const *jobs, int32_t njobs, ea_sp_batch **out) {
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->bs, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+  b->all.jobs = b->jobs;
+  for (ea_sp *c : b->jobs) b->all.ncol_max = std::max(b->all.ncol_max, c->d.ncol);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&b->all.d_jobs, sizeof(SpDev) * b->jobs.size());
+  if (e == cudaSuccess) e = cudaMalloc((void **)&b->all.d_pre, sizeof(uint32_t) * SPB_COUNT * (b->jobs.size() + 1));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&b->p_bar, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc((void **)&b->p_err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(b->p_err, 0, sizeof(int));
   for (SpClass &k : b->classes) {
     const size_t n = k.jobs.size();
     if (e == cudaSuccess) e = cudaMalloc((void **)&k.d_jobs, sizeof(SpDev) * n);
@@ -1540,6 +1829,10 @@ int ea_sp_batch_destroy(ea_sp_batch *b) {
     if (k.join) cudaEventDestroy(k.join);
     if (k.fs) cudaStreamDestroy(k.fs);
   }
+  if (b->all.d_jobs) cudaFree(b->all.d_jobs);
+  if (b->all.d_pre) cudaFree(b->all.d_pre);
+  if (b->p_bar) cudaFree(b->p_bar);
+  if (b->p_err) cudaFree(b->p_err);
   if (b->done) cudaEventDestroy(b->done);
   if (b->fork) cudaEventDestroy(b->fork);
   if (b->bs) cudaStreamDestroy(b->bs);
@@ -1557,6 +1850,12 @@ int ea_sp_batch_sync(ea_sp_batch *b) {
   if (!b) return spfail(EA_ERR_ARG, "null batch");
   SCU(cudaSetDevice(b->device));
   SCU(cudaStreamSynchronize(b->bs));
+  return sp_check_persist(b->p_err, b->bs);
+}
+
+int ea_sp_batch_set_bin_kernel(ea_sp_batch *b, int32_t mode) {
+  if (!b || mode < EA_BIN_AUTO || mode > EA_BIN_PERSISTENT) return spfail(EA_ERR_ARG, "bad bin-kernel mode");
+  b->bin_mode = mode;
   return EA_OK;
 }
 
@@ -1573,6 +1872,28 @@ int ea_sp_batch_run(ea_sp_batch *b, const ea_cadence *cad) {
     SCU(cudaEventRecord(b->done, c->st));
     SCU(cudaStreamWaitEvent(b->bs, b->done, 0));
   }
+  bool persist = b->bin_mode == EA_BIN_PERSISTENT;
+  if (b->bin_mode == EA_BIN_AUTO) {
+    persist = b->jobs.size() > 1;
+    for (ea_sp *c : b->jobs) persist = persist && sp_small(c->d);
+  }
+  if (persist) {
+    // one work list of every job, one cooperative launch per bin
+    if ((rc = spb_upload(b->all, cad->cluster != 0, b->bs))) return rc;
+    for (ea_sp *c : b->jobs)
+      SCU(cudaMemsetAsync(c->d.avgE, 0, sizeof(double) * (size_t)c->d.nw * 64 * c->d.NR * c->d.NB, b->bs));
+    SpPersistDev p{};
+    p.b = b->all.bd;
+    p.itmax = cad->itmax; p.houfr = cad->houfr; p.mesfr = cad->mesfr; p.ptfr = cad->ptfr;
+    p.cluster = cad->cluster != 0;
+    p.ncol_max = b->all.ncol_max;
+    p.bar = b->p_bar;
+    p.err = b->p_err;
+    const size_t smem = (size_t)std::max(std::max(p.b.pass_smem, p.b.perm_smem), p.b.cluster_smem);
+    const int grid = sp_persist_grid(p.b, smem);
+    if (grid < 1) return spfail(EA_ERR_CUDA, "persistent bin kernel: no co-resident grid for %zu bytes of shared memory", smem);
+    SCU(sp_launch_persist(p, grid, smem, b->bs));
+  } else {
   std::vector<SpBatchDev> bds;
   for (SpClass &k : b->classes) {
     if ((rc = spb_upload(k, cad->cluster != 0, b->bs))) return rc;
@@ -1604,6 +1925,7 @@ int ea_sp_batch_run(ea_sp_batch *b, const ea_cadence *cad) {
     b->it_bd = bds;
   }
   for (int it = 0; it < cad->itmax; ++it) SCU(cudaGraphLaunch(b->it_graph, b->bs));
+  }
   // later work of each job comes after the batch
   SCU(cudaEventRecord(b->done, b->bs));
   for (ea_sp *c : b->jobs) {

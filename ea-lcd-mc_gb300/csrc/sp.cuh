@@ -114,6 +114,17 @@ struct SpBatchDev {
   int cluster_threads;                      // block size of the labelling
 };
 void sp_batch_blocks(const SpDev &d, bool cluster, uint32_t out[SPB_COUNT]);
+
+// Persistent bin kernel (k_sp_persist): whole bins of the jobs of a work
+// list in one cooperative launch.
+struct SpPersistDev {
+  SpBatchDev b;
+  int itmax, houfr, mesfr, ptfr, cluster, ncol_max;
+  unsigned long long *bar;  // arrivals at the grid barrier (zeroed by sp_launch_persist)
+  int *err;                 // barrier waits that gave up (zero at set-up; read by the host)
+};
+int sp_persist_grid(const SpBatchDev &b, size_t smem);
+cudaError_t sp_launch_persist(const SpPersistDev &p, int grid, size_t smem, cudaStream_t st);
 cudaError_t sp_batch_setup();
 cudaError_t sp_batch_sweep(const SpBatchDev &b, int ncol_max, cudaStream_t st);
 cudaError_t sp_batch_tempering(const SpBatchDev &b, cudaStream_t st);

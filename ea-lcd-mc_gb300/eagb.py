@@ -46,6 +46,7 @@ class ServerConfig(C.Structure):
 
 
 EA_LAYOUT_MULTISPIN, EA_LAYOUT_SAMPLE_PACKED = 0, 1
+EA_BIN_AUTO, EA_BIN_GRAPH, EA_BIN_PERSISTENT = 0, 1, 2
 
 
 class Request(C.Structure):
@@ -509,6 +510,10 @@ class SpJob:
     def sync(self):
         _ck(lib().ea_sp_sync(self.h))
 
+    def set_bin_kernel(self, mode):
+        """EA_BIN_AUTO, EA_BIN_GRAPH or EA_BIN_PERSISTENT (ea_sp_set_bin_kernel)."""
+        _ck(lib().ea_sp_set_bin_kernel(self.h, int(mode)))
+
     def get_spins(self):
         S = np.zeros((self.g.nwords, self.V, self.g.nrep, self.g.nbetas), np.uint64)
         _ck(lib().ea_sp_get_spins(self.h, P(S)))
@@ -602,6 +607,9 @@ class SpBatch:
     def run_bin(self, itmax, houfr=1, mesfr=1, ptfr=1, cluster=False, nclust=0):
         cad = Cadence(itmax, houfr, mesfr, ptfr, int(cluster), nclust)
         _ck(lib().ea_sp_batch_run(self.b, C.byref(cad)))
+
+    def set_bin_kernel(self, mode):
+        _ck(lib().ea_sp_batch_set_bin_kernel(self.b, int(mode)))
 
     def sync(self):
         _ck(lib().ea_sp_batch_sync(self.b))

@@ -163,22 +163,28 @@ int ea_monte_carlo(ea_ctx *ctx, int32_t nsweeps);
 /* Measure_Energy (main.cu:531-554).  out may be NULL (result stays on the device). */
 int ea_measure_energy(ea_ctx *ctx, int32_t *out);
 /* Energy measurement that allocates nothing.  No counterpart in the reference:
- * it exists for callers that cannot call cudaMalloc -- code recording into a
- * CUDA graph while a stream capture is active, frameworks that hand out every
- * device byte from their own pool, and loops that cannot take the device
- * synchronisation of an allocation.  Same result as ea_measure_energy for
+ * it exists for callers that cannot call cudaMalloc -- frameworks that hand
+ * out every device byte from their own pool (a cudaMalloc behind their back
+ * breaks their accounting and can fail when the pool holds the memory), and
+ * loops that cannot take the device-wide synchronisation an allocation may
+ * imply.  Same result as ea_measure_energy for
  * spins [nsamples][2][NB][half][NR] and couplings [nsamples][2][6][half]
  * already in device memory; writes energies [nsamples][NR][NB] (int32) to
  * d_energies on `stream` (a cudaStream_t, NULL = legacy default stream), on
- * the calling thread's current device.  Its scratch is a fixed 4.4 MiB device
- * array inside the library (held by every GPU that loads it until exit), so
- * it rejects, with EA_ERR_ARG and a message, jobs beyond
+ * the calling thread's current device.  NR must be 2, 4 or 8 (the tile
+ * widths KT = 16, 8, 4 of the energy kernel); other replica counts get
+ * EA_ERR_ARG.  Its scratch is a fixed 4.4 MiB device array inside the
+ * library (held by every GPU that loads it until exit), so it rejects, with
+ * EA_ERR_ARG and a message, jobs beyond
  * (L/4)^2 (Lz/4) / 2 <= 8192 half-sites and
  * ceil(half/KT) * nsamples * NB * NR <= 2^20 partial sums (KT = 32/NR).
- * The first call on each device looks up the array's device address; make
- * that first call before any stream capture.  All calls share the array, so
- * calls whose kernels overlap on the GPU race; serialise them (one stream, or
- * events).  Nothing in the array needs to start at zero. */
+ * The first call on each device (and the first after that device's context
+ * is recreated, e.g. by cudaDeviceReset) looks up the array's device address;
+ * make that first call before any stream capture.  All calls share the array,
+ * so calls whose kernels overlap on the GPU race; serialise them (one stream,
+ * or events).  Nothing in the array needs to start at zero.  A CUDA error
+ * already pending on the calling thread when it is called is reported (and
+ * left pending) instead of being taken for a failure of this call. */
 int ea_measure_energy_noalloc(const ea_geom *g, const uint64_t *d_spins, const uint64_t *d_couplings,
                               int32_t *d_energies, void *stream);
 /* Parallel_Tempering for every (sample, replica) (upd.c:3-48) on the device, with
@@ -254,6 +260,12 @@ int ea_check_exact(ea_ctx *ctx);
 enum { EA_K_SWEEP = 0, EA_K_PT = 1, EA_K_CLUSTER = 2, EA_K_ENERGY = 3, EA_K_RNG = 4, EA_K_COUNT = 5 };
 int ea_profile(ea_ctx *ctx, int32_t on);
 int ea_kernel_time(ea_ctx *ctx, int32_t kind, int64_t *launches, double *total_ms);
+/* Measured peak rate of 32-bit integer instructions on a device, in thread
+ * operations per second over all SMs: independent xor/add chains
+ * (alu_ops_per_s) and multiply-add chains (imad_ops_per_s; either pointer
+ * may be NULL).  No counterpart in the reference: it is the denominator of
+ * the integer-pipe roofline of the sweep kernels. */
+int ea_probe_int32_rate(int32_t device, double *alu_ops_per_s, double *imad_ops_per_s);
 
 /* A new run (flag 1 of the reference) on an existing context, as Init() does
  * (ini.c:32-101, 316-383, 465-730, 763-781): seeds from the four master seeds
@@ -341,6 +353,19 @@ int ea_sp_houdayer(ea_sp *job, int32_t nclust);
 int ea_sp_run(ea_sp *job, const ea_cadence *cad, double *avgE);
 /* The last bin's average energies (by ea_sp_run or a batch), as ea_sp_run returns them. */
 int ea_sp_bin_results(ea_sp *job, double *avgE);
+/* How ea_sp_run (and ea_sp_batch_run) executes a bin.  EA_BIN_GRAPH: one
+ * bin iteration replayed as a CUDA graph of one launch per phase (colour
+ * pass, energy, tempering, permute, labelling, ...).  EA_BIN_PERSISTENT: one
+ * cooperative launch of a persistent kernel runs the whole bin, the same
+ * phase bodies in the same order separated by grid barriers, so the results
+ * are identical; it removes the per-phase launch gaps that bound jobs too
+ * small to fill the GPU.  A barrier wait gives up after 4 s (the kernel
+ * returns) and the next ea_sp_sync / ea_sp_bin_results / ea_sp_batch_sync
+ * reports EA_ERR_CUDA.  EA_BIN_AUTO (default): a job alone takes the graph;
+ * a batch of two or more jobs takes the persistent kernel when every job has
+ * at most 2^20 spin words (nwords x V x NR x NB), the graph otherwise. */
+enum { EA_BIN_AUTO = 0, EA_BIN_GRAPH = 1, EA_BIN_PERSISTENT = 2 };
+int ea_sp_set_bin_kernel(ea_sp *job, int32_t mode);
 /* Batches of sample-packed jobs (any geometries, replica and temperature
  * counts, up to 4 colours each).  Jobs are grouped in classes (one per job
  * for up to 256 jobs, else of equal NB and similar lattice size); each class
@@ -355,6 +380,8 @@ int ea_sp_batch_run(ea_sp_batch *b, const ea_cadence *cad);
 int ea_sp_batch_sync(ea_sp_batch *b);
 int ea_sp_batch_stream(ea_sp_batch *b, void **stream);
 int ea_sp_batch_destroy(ea_sp_batch *b);
+/* EA_BIN_* for the batch's bins (see ea_sp_set_bin_kernel). */
+int ea_sp_batch_set_bin_kernel(ea_sp_batch *b, int32_t mode);
 /* Exact enumeration (V <= 32): dos [nwords*64][6V+1] configurations with
  * spin 0 up at each E = -3V..3V, and meanE [nwords*64][nbeta] = <E>(beta)
  * from it in FP64 on the GPU. */

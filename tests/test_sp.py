@@ -403,3 +403,105 @@ def test_large_batch_classes_equal_jobs_alone():
     batch.close()
     for j in alone + batched:
         j.close()
+
+
+def oracle_bin(orc, itmax, houfr, mesfr, ptfr, cluster, nclust=0):
+    """One bin of the cadence on the oracle: sweeps, tempering every ptfr
+    sweeps, a move every houfr tempering steps, the energy measured after
+    each of the itmax iterations; returns the averages."""
+    tot = np.zeros((orc.nw, 64, orc.NR, orc.NB))
+    for it in range(itmax):
+        for im in range(mesfr):
+            for ih in range(houfr):
+                orc.sweeps(ptfr)
+                orc.pt()
+            if cluster:
+                orc.houdayer(nclust)
+        tot += 3 * orc.V - orc.energy()
+    return tot / itmax
+
+
+# the sample-packed configurations the bench times, at the size it times them:
+# L=6, Lz=24, PBC, NT=12 in [0.8, 1.6], NR=2, one word (64 samples), a bin
+# of 512 sweeps with tempering after each (no cluster moves); and L=12,
+# Lz=48, OBC, NT=24 in [0.7, 1.6], NR=4, 64 words (4096 samples), a bin of 10
+# sweeps with tempering after each and a Houdayer move on the colder half --
+# the 16-byte two-slot pass, the tile width, the energy chunking and the
+# 4-samples-per-pass labelling of 6912-site lattices as the bench runs them
+TIMED = [(6, 24, eagb.EA_PBC, "T08_16_N12", 2, 1, (512, 1, 1, 1, False)),
+         (12, 48, eagb.EA_OBC, "T07_16_N24", 4, 1, (10, 10, 1, 1, True)),
+         (12, 48, eagb.EA_OBC, "T07_16_N24", 4, 64, (1, 10, 1, 1, True))]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("L,Lz,bc,ln,NR,nw,cad", TIMED)
+def test_timed_configurations_match_oracle(L, Lz, bc, ln, NR, nw, cad):
+    itmax, houfr, mesfr, ptfr, cl = cad
+    job = new_job(L, Lz, bc, ln, NR, nw, jobid=0)
+    orc = OracleSP(job, 0)
+    avg = job.run_bin(itmax, houfr, mesfr, ptfr, cluster=cl, nclust=0)
+    want = oracle_bin(orc, itmax, houfr, mesfr, ptfr, cl)
+    assert np.array_equal(job.get_spins(), orc.S)
+    assert np.array_equal(avg, want)
+    gE, gperm, gacc, gM = job.tempering()
+    assert np.array_equal(gperm, orc.perm) and np.array_equal(gacc, orc.acc)
+    assert job.counter() == (orc.it, orc.step)
+    assert orc.acc.sum() > 0
+    job.close()
+
+
+# jobs of 2 and 3 colours, 1..3 words, 2..5 replicas, with and without moves
+BINS = [(6, 8, eagb.EA_PBC, "T08_16_N4", 2, 2, (3, 2, 1, 2, False)),
+        (5, 7, eagb.EA_OBC, "T07_16_N6", 4, 1, (2, 2, 2, 1, True)),
+        (7, 4, eagb.EA_PBC, "T07_16_N8:7", 5, 3, (2, 3, 1, 1, True)),
+        (12, 16, eagb.EA_OBC, "T07_16_N12", 4, 2, (2, 5, 1, 1, True))]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("L,Lz,bc,ln,NR,nw,cad", BINS)
+def test_persistent_bin_kernel_equals_graph(L, Lz, bc, ln, NR, nw, cad):
+    """The persistent bin kernel (one cooperative launch per bin) and the
+    graph of per-phase launches give the same words, averages, tempering
+    state and counters, bin after bin; and both equal the oracle."""
+    itmax, houfr, mesfr, ptfr, cl = cad
+    a, b = new_job(L, Lz, bc, ln, NR, nw, jobid=11), new_job(L, Lz, bc, ln, NR, nw, jobid=11)
+    a.set_bin_kernel(eagb.EA_BIN_GRAPH)
+    b.set_bin_kernel(eagb.EA_BIN_PERSISTENT)
+    orc = OracleSP(a, 11)
+    for _ in range(2):
+        va = a.run_bin(itmax, houfr, mesfr, ptfr, cluster=cl)
+        vb = b.run_bin(itmax, houfr, mesfr, ptfr, cluster=cl)
+        want = oracle_bin(orc, itmax, houfr, mesfr, ptfr, cl)
+        assert np.array_equal(va, want) and np.array_equal(vb, want)
+    assert np.array_equal(a.get_spins(), b.get_spins())
+    assert np.array_equal(b.get_spins(), orc.S)
+    assert all(np.array_equal(x, y) for x, y in zip(a.tempering(), b.tempering()))
+    assert a.counter() == b.counter() == (orc.it, orc.step)
+    a.close()
+    b.close()
+
+
+@pytest.mark.gpu
+def test_persistent_batch_equals_graph_batch():
+    """A batch of mixed jobs run by the persistent bin kernel (one work list
+    of every job) ends as the same batch run by per-class graph branches."""
+    geoms = BATCH + [(12, 16, eagb.EA_OBC, "T07_16_N12", 4, 2), (3, 5, eagb.EA_PBC, "T07_16_N8", 2, 1)]
+    ga = [new_job(*c, jobid=60 + k) for k, c in enumerate(geoms)]
+    gb = [new_job(*c, jobid=60 + k) for k, c in enumerate(geoms)]
+    A, B = eagb.SpBatch(ga), eagb.SpBatch(gb)
+    A.set_bin_kernel(eagb.EA_BIN_GRAPH)
+    B.set_bin_kernel(eagb.EA_BIN_PERSISTENT)
+    for itmax, houfr, mesfr, ptfr, cl in [(2, 2, 1, 1, True), (3, 1, 2, 2, False)]:
+        A.run_bin(itmax, houfr, mesfr, ptfr, cluster=cl)
+        B.run_bin(itmax, houfr, mesfr, ptfr, cluster=cl)
+        A.sync()
+        B.sync()
+        for x, y in zip(ga, gb):
+            assert np.array_equal(x.bin_results(), y.bin_results())
+    for x, y in zip(ga, gb):
+        assert np.array_equal(x.get_spins(), y.get_spins())
+        assert x.counter() == y.counter()
+    A.close()
+    B.close()
+    for j in ga + gb:
+        j.close()
