@@ -32,8 +32,8 @@ LUT = os.path.join(ROOT, "tests", "golden", "lut_T06_16_N32.npz")
 MASTERS = (0x1234567890ABCDEF, 0x0FEDCBA987654321, 0x1111222233334444, 0x5555666677778888)
 WORKLOAD = "L24_Lz192_OBC_NB32_NR8_ns31_ptfr1_houfr5"
 # DRAM bytes (read + write) of one k_sweep launch of this workload, from the
-# ncu capture of the bench's k_sweep launches (mean of two launches)
-KSWEEP_DRAM_BYTES = 136.0e6
+# ncu capture of one k_sweep launch of the bench (its full-set capture)
+KSWEEP_DRAM_BYTES = 140.6e6
 # The integer-op model of the fused sweep (the Philox4x32-10 rounds, the
 # post-mix and rotation of a random word, the threshold search per byte, the
 # bit-sliced update per word), in 32-bit operations: 6 Philox calls of
@@ -367,7 +367,8 @@ def serve_sp_stream(njobs, seed=9):
     return jobs
 
 
-def run_serve_stream(dev, eagb, stream, sweeps_per_bin, submit_kw, su_of, capacity, util, workload, seed):
+def run_serve_stream(dev, eagb, stream, sweeps_per_bin, submit_kw, su_of, capacity, util, workload, seed,
+                     t_limit=600.0):
     """A Poisson stream of jobs through a server: p50/p99 completion latency
     and spin-updates/ps of the completed work."""
     import threading
@@ -399,7 +400,7 @@ def run_serve_stream(dev, eagb, stream, sweeps_per_bin, submit_kw, su_of, capaci
     # a finished job holds its bytes until released: release each as soon as
     # it is done, whatever the order
     done = [False] * njobs
-    t_limit = time.perf_counter() + 600.0
+    t_limit = time.perf_counter() + t_limit
     while not all(done) and time.perf_counter() < t_limit:
         for k in range(njobs):
             if done[k] or tickets[k] is None:
@@ -424,7 +425,41 @@ def run_serve_stream(dev, eagb, stream, sweeps_per_bin, submit_kw, su_of, capaci
             "span_s": st["span_s"], "completed": st["completed"], "failed": st["failed"],
             "peak_running": st["peak_running"], "bins": st["bins"], "batch_changes": st["batch_changes"],
             "hbm_budget": st["budget"], "hbm_peak": st["bytes_peak"], "gpu_busy_s": st["gpu_busy_s"],
-            "host_enqueue_s": st["enqueue_s"], "host_admit_s": st["admit_s"]}
+            "host_enqueue_s": st["enqueue_s"], "host_admit_s": st["admit_s"],
+            "latency_components_ms": {k: st[k + "_ms"] for k in
+                                      ("queue_p50", "queue_p99", "prep_p50", "prep_p99", "start_p50", "start_p99",
+                                       "run_p50", "run_p99", "gpu_p50", "gpu_p99")}}
+
+
+# the serving configuration at its stated size: L uniform in 6..20, Lz/L in
+# {1,2,4,8,16}, PBC/OBC, NT in {8..32}, 64 samples per job, NR=4, a Houdayer
+# move every 10 sweeps, sweeps log-uniform in 2^14..2^20 (bins of 100 sweeps);
+# a bounded number of jobs drawn from it (a job averages ~2e13 spin updates)
+SERVE_C5_WORKLOAD = "poisson_L6-20_LzL1-16_PBC-OBC_NT8-32_NR4_64samples_houfr10_sweeps2^14-2^20"
+
+
+def serve_c5_stream(njobs, seed=5):
+    rng = np.random.default_rng(seed)
+    jobs = []
+    for k in range(njobs):
+        L = int(rng.integers(6, 21))
+        Lz = L * int(rng.choice([1, 2, 4, 8, 16]))
+        bc = int(rng.integers(0, 2))
+        nt = int(rng.choice(SERVE_NT))
+        sweeps = int(round(2.0 ** rng.uniform(14, 20)))
+        jobs.append((L, Lz, bc, nt, max(1, int(round(sweeps / 100.0)))))
+    return jobs
+
+
+def run_serve_c5(args, dev, eagb, njobs, util=0.8):
+    stream = serve_c5_stream(njobs)
+    kw = dict(nsamples=1, NR=SERVE_NR, itmax=10, houfr=10, mesfr=1, ptfr=1, cluster=True,
+              layout=eagb.EA_LAYOUT_SAMPLE_PACKED, nwords=1)
+    su_of = lambda L, Lz, bc, nt, nb: 100 * nb * L * L * Lz * SERVE_NR * nt * 64
+    rec = run_serve_stream(dev, eagb, stream, 100, kw, su_of, 0.5e12, util, SERVE_C5_WORKLOAD, 17,
+                           t_limit=3600.0)
+    rec["jobs_drawn"] = [{"L": L, "Lz": Lz, "bc": bc, "nt": nt, "sweeps": 100 * nb} for L, Lz, bc, nt, nb in stream]
+    return rec
 
 
 def run_serve_sp(args, dev, eagb, njobs=100, util=0.8):
@@ -451,6 +486,8 @@ SP_CASES = [
     ("L6_Lz24_PBC_NT12_NR2_64samples_ptfr1", 6, 24, 0, "T08_16_N12", 2, 1, (512, 1, 1, False), 8),
     ("L12_Lz48_OBC_NT24_NR4_64samples_houfr10", 12, 48, 1, "T07_16_N24", 4, 1, (10, 10, 1, True), 10),
     ("L12_Lz48_OBC_NT24_NR4_4096samples_houfr10", 12, 48, 1, "T07_16_N24", 4, 64, (2, 10, 1, True), 10),
+    # the large tube as written: NR=4, 64 samples per word, Houdayer every 5 sweeps on the colder half
+    ("L24_Lz192_OBC_NT32_NR4_64samples_houfr5", 24, 192, 1, "T06_16_N32", 4, 1, (1, 5, 1, True), 10),
 ]
 
 
@@ -567,6 +604,51 @@ def run_mixed_sp(args, dev, torch, eagb, nwords=SPMIX_WORDS, steps=2):
             "bit_exact_plain_vs_batched": bool(same),
             "graph": "one bin iteration of the batch replayed as a CUDA graph",
             "l2": "spin words %.2f GB against a 129 MB L2" % (spin_bytes / 1e9)}
+
+
+def run_no_cluster(args, dev, torch, eagb):
+    """The headline geometry without cluster moves: one step = 5 x (sweep +
+    energy + parallel tempering) + the energy measurement, so the fused sweep
+    is most of the step (the cluster uniforms, which bound the full step, are
+    not drawn).  Device-timed, L2 flushed between steps."""
+    d = np.load(LUT)
+    betas, cum = d["betas"], d["cum"]
+    NB = len(betas)
+    job = eagb.new_job(L, LZ, betas, cum, nsamples=NS, NR=NR, bc=eagb.EA_OBC, masters=MASTERS, device=dev, jobid=1)
+    job.set_rng_sms(0)
+    stream = torch.cuda.ExternalStream(job.stream(), device=dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.int32, device=dev)
+    cad = dict(itmax=1, houfr=HOUFR, mesfr=1, ptfr=1, cluster=False)
+    for _ in range(args.warmup):
+        job.run_cycles(**cad)
+    job.sync()
+    eagb._ck(eagb.lib().ea_profile(job.ctx, 1))
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            flush.fill_(i)
+            evs[i][0].record(stream)
+            job.run_cycles(**cad)
+            evs[i][1].record(stream)
+    job.sync()
+    ms = sum(a.elapsed_time(b) for a, b in evs)
+    nsw, sw_ms = C.c_int64(), C.c_double()
+    eagb._ck(eagb.lib().ea_kernel_time(job.ctx, 0, C.byref(nsw), C.byref(sw_ms)))
+    eagb._ck(eagb.lib().ea_profile(job.ctx, 0))
+    job.close()
+    su = HOUFR * L * L * LZ * NR * NB * NS * args.steps
+    half = (L // 4) ** 2 * (LZ // 4) // 2
+    words = NS * NB * half * NR
+    launch_ms = sw_ms.value / max(1, nsw.value)
+    ops, e = int_ops(cum, NB * half * NR, words)
+    ipk = int_peak(eagb, dev)[0]
+    hbm, _ = peaks()
+    return {"workload": WORKLOAD.replace("_houfr5", "_no_cluster"), "value": su / (ms * 1e-3) / 1e12,
+            "unit": "spin-updates/ps", "ms_per_step": ms / args.steps, "sweep_launch_ms": launch_ms,
+            "sweep_share": sw_ms.value / ms,
+            "sweep_int_frac": ops / (launch_ms * 1e-3) / ipk,
+            "sweep_hbm_frac": (words * 24 + NS * 6 * half * 8) / (launch_ms * 1e-3) / 1e9 / hbm,
+            "l2": "flushed between steps (512 MB write)"}
 
 
 def run_ours(args, rank, world, local):
@@ -729,6 +811,7 @@ def run_ours(args, rank, world, local):
                       "uniforms_overlapped": rg_ms.value, "step_total": ms},
         "clocks": clk.summary(),
     }
+    line["no_cluster"] = run_no_cluster(args, dev, torch, eagb)
     if not args.no_mixed:
         line["batched"] = [run_mixed(args, dev, torch, eagb, 4, 8), run_mixed(args, dev, torch, eagb, 32, 1),
                            run_mixed_sp(args, dev, torch, eagb), run_mixed_sp(args, dev, torch, eagb, 72, 10)]
@@ -762,6 +845,8 @@ def main():
                     help="only two bins of the 36-job x 32-sample multispin mix in this form (for profilers)")
     ap.add_argument("--rng-sms", type=int, default=-1,
                     help="SMs of the cluster-uniform generator's partition for the headline job (-1: automatic)")
+    ap.add_argument("--serve-config5", type=int, default=0, metavar="N",
+                    help="only the serving configuration at its stated size: N jobs drawn from it (prints its record)")
     ap.add_argument("--sp-case", default="", help="run only the sample-packed workloads whose name contains this "
                     "(--steps bins after --warmup; prints their JSON records)")
     args = ap.parse_args()
@@ -791,6 +876,8 @@ def main():
                 j.sync()
         for j in jobs:
             j.close()
+    elif args.serve_config5:
+        print(json.dumps(run_serve_c5(args, local, load_eagb(), args.serve_config5)), flush=True)
     elif args.sp_case:
         import torch
         print(json.dumps(run_sp(args, local, torch, load_eagb())), flush=True)

@@ -110,7 +110,7 @@ int own(ea_ctx *c, T *&p, size_t n) {
 
 int choose_kt(const Geometry &g) {
   const char *env = getenv("EAGB_KT");
-  auto smem = [&](int kt) { return (size_t)g.NB * 2560 + (size_t)3 * g.NB * kt * g.NR * 8 + (size_t)kt * 32; };
+  auto smem = [&](int kt) { return sweep_smem_for(g.NB, g.NR, kt); };
   const int cands_nr8[3] = {4, 2, 1}, cands_nr4[3] = {8, 4, 2}, cands_nr2[3] = {16, 8, 4};
   const int *c = g.NR == 8 ? cands_nr8 : g.NR == 4 ? cands_nr4 : cands_nr2;
   if (env) {
@@ -1002,7 +1002,7 @@ static int set_tile(ea_ctx *c, int kt) {
   JobDev &j = c->j;
   if (kt == j.kt) return EA_OK;
   const Geometry &g = c->g;
-  const size_t smem = (size_t)g.NB * 2560 + (size_t)3 * g.NB * kt * g.NR * 8 + (size_t)kt * 32;
+  const size_t smem = sweep_smem_for(g.NB, g.NR, kt);
   if (smem > 227 * 1024) return fail(EA_ERR_ARG, "tile width %d needs %zu bytes of shared memory", kt, smem);
   const int nt = (g.half + kt - 1) / kt;
   if (nt > j.ntiles) {

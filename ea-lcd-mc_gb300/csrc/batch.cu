@@ -218,9 +218,7 @@ cudaError_t batch_setup(int NR, int KT) {
   }
 }
 
-int batch_sweep_smem(int NR, int KT, int NBmax) {
-  return NBmax * 256 * (8 + 2) + 3 * NBmax * KT * NR * 8 + KT * 8 * 4;
-}
+int batch_sweep_smem(int NR, int KT, int NBmax) { return (int)sweep_smem_for(NBmax, NR, KT); }
 
 cudaError_t batch_fill_bits(const BatchDev &b, int parity, cudaStream_t st) {
   kb_fill_bits<<<b.njobs, 64, 0, st>>>(b, parity);

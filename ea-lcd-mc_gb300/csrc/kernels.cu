@@ -26,7 +26,7 @@ void set_dividers(JobDev &j) {
 __global__ void k_fill_bits(const __grid_constant__ JobDev j, int parity) { fill_bits_body(j, parity); }
 
 template <int NR, int KT, bool UPDATE>
-__global__ void __launch_bounds__(512) k_sweep(const __grid_constant__ JobDev j, int parity, int energy) {
+__global__ void __launch_bounds__(512, 3) k_sweep(const __grid_constant__ JobDev j, int parity, int energy) {
   extern __shared__ __align__(16) unsigned char smem[];
   sweep_body<NR, KT, UPDATE>(j, blockIdx.x, parity, energy, smem);
 }
@@ -169,9 +169,7 @@ __global__ void k_cc_flatten(JobDev j) {
 // ---------------------------------------------------------------------------
 int sweep_kt(const JobDev &j) { return j.kt; }
 
-size_t sweep_smem_bytes(const JobDev &j) {
-  return (size_t)j.NB * 256 * (8 + 2) + (size_t)3 * j.NB * j.kt * j.NR * 8 + (size_t)j.kt * 8 * 4;
-}
+size_t sweep_smem_bytes(const JobDev &j) { return sweep_smem_for(j.NB, j.NR, j.kt); }
 
 template <int NR, int KT>
 static cudaError_t launch_sweep_t(const JobDev &j, int parity, bool energy, bool update, cudaStream_t st) {

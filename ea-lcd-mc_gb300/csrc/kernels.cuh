@@ -95,6 +95,12 @@ void set_dividers(JobDev &j);
 // Tile width (half-sites per CTA) of the fused sweep kernel.
 int sweep_kt(const JobDev &j);
 size_t sweep_smem_bytes(const JobDev &j);
+// Dynamic SMEM of a fused half-sweep CTA: the random triples of the tile
+// (3 x NB x KT x NR words), the pre-search tables (NB x 256 x 2 B) and the
+// tile's neighbour records (KT x 8 ints).
+inline size_t sweep_smem_for(int NB, int NR, int KT) {
+  return (size_t)3 * NB * KT * NR * 8 + (size_t)NB * 256 * 2 + (size_t)KT * 8 * 4;
+}
 
 cudaError_t launch_fill_bits(const JobDev &j, int parity, cudaStream_t st);
 cudaError_t launch_sweep(const JobDev &j, int parity, bool energy, cudaStream_t st);

@@ -59,7 +59,8 @@ struct Job {
   int rc = EA_OK;
   std::string err;
   int bins_done = 0, bins_queued = 0;
-  double t_submit = -1, t_admit = -1, t_done = -1;
+  double t_submit = -1, t_admit = -1, t_done = -1, t_ready = -1, t_start = -1;
+  double gpu_s = 0;  // device time of its bins (worker only)
   uint64_t bytes = 0;
   int passed = 0;  // times a later request was admitted ahead of this one
   bool freeing = false;  // handed to the reaper
@@ -81,6 +82,7 @@ using ClassKey = std::tuple<int, int, int, int, int, int, int>;
 
 struct InFlight {
   cudaEvent_t ev0, ev;  // around the bin on the batch stream
+  std::vector<Job *> members;    // jobs of the bin
   std::vector<Job *> finishing;  // jobs whose last bin this is
 };
 
@@ -183,7 +185,10 @@ void retire(ea_server *s, bool block) {
         }
       }
       float ms = 0.f;
-      if (q == cudaSuccess && cudaEventElapsedTime(&ms, f.ev0, f.ev) == cudaSuccess) s->gpu_busy_s += 1e-3 * ms;
+      if (q == cudaSuccess && cudaEventElapsedTime(&ms, f.ev0, f.ev) == cudaSuccess) {
+        s->gpu_busy_s += 1e-3 * ms;
+        for (Job *j : f.members) j->gpu_s += 1e-3 * ms;
+      }
       s->ev_pool.push_back(f.ev0);
       s->ev_pool.push_back(f.ev);
       g->inflight.pop_front();
@@ -218,14 +223,15 @@ Group *group_for(ea_server *s, Job *j) {
   return g;
 }
 
-// Widest sweep tile width for NR replicas whose shared memory (thresholds and
-// pre-search of every temperature, three random words per tile site and
-// replica and temperature, energy slots) holds nb_max temperatures.
+// Widest sweep tile width for NR replicas whose shared memory (three random
+// words per tile site, replica and temperature, the pre-search of every
+// temperature, the tile's neighbour records: sweep_smem_for in kernels.cuh)
+// holds nb_max temperatures.
 int tile_for(int NR, int nb_max) {
   const int c8[3] = {4, 2, 1}, c4[3] = {8, 4, 2}, c2[3] = {16, 8, 4};
   const int *c = NR == 8 ? c8 : NR == 4 ? c4 : c2;
   for (int i = 0; i < 3; ++i)
-    if (nb_max * 256 * 10 + 3 * nb_max * c[i] * NR * 8 + c[i] * 32 <= 227 * 1024 - 256) return c[i];
+    if (3 * nb_max * c[i] * NR * 8 + nb_max * 256 * 2 + c[i] * 32 <= 227 * 1024 - 256) return c[i];
   return c[2];
 }
 
@@ -326,6 +332,7 @@ void prep_main(ea_server *s) {
       finish(s, j, rc, e);
       continue;
     }
+    j->t_ready = s->now();
     s->ready_q.push_back(j);
     s->cv.notify_all();
   }
@@ -400,7 +407,10 @@ bool step_group(ea_server *s, Group *g) {
   std::vector<Job *> stay;
   {
     std::lock_guard<std::mutex> lk(s->m);
+    const double t = s->now();
+    f.members = g->members;
     for (Job *j : g->members) {
+      if (j->t_start < 0) j->t_start = t;
       ++j->bins_done;
       if (j->bins_done >= j->req.nbins) f.finishing.push_back(j);
       else stay.push_back(j);
@@ -594,6 +604,9 @@ int ea_server_info(ea_server *s, int64_t ticket, ea_job_info *info) {
   info->t_submit = j->t_submit;
   info->t_admit = j->t_admit;
   info->t_done = j->t_done;
+  info->t_ready = j->t_ready;
+  info->t_start = j->t_start;
+  info->gpu_s = j->gpu_s;
   info->bytes = j->bytes;
   info->spin_updates = j->su();
   return EA_OK;
@@ -665,6 +678,28 @@ int ea_server_stats(ea_server *s, ea_serve_stats *st) {
   st->gpu_busy_s = s->gpu_busy_s;
   st->enqueue_s = s->enqueue_s;
   st->admit_s = s->admit_s;
+  // latency components of the completed jobs
+  std::vector<double> cq, cp, cs, cr, cg;
+  for (auto &kv : s->jobs) {
+    const Job *j = kv.second.get();
+    if (j->t_done < 0 || j->rc != EA_OK || j->t_start < 0) continue;
+    cq.push_back(1e3 * (j->t_admit - j->t_submit));
+    cp.push_back(1e3 * (j->t_ready - j->t_admit));
+    cs.push_back(1e3 * (j->t_start - j->t_ready));
+    cr.push_back(1e3 * (j->t_done - j->t_start));
+    cg.push_back(1e3 * j->gpu_s);
+  }
+  auto pct_of = [](std::vector<double> v, double p) {
+    if (v.empty()) return 0.0;
+    std::sort(v.begin(), v.end());
+    size_t k = (size_t)std::ceil(p * (double)v.size());
+    return v[std::min(v.size(), std::max<size_t>(k, 1)) - 1];
+  };
+  st->queue_p50_ms = pct_of(cq, 0.5); st->queue_p99_ms = pct_of(cq, 0.99);
+  st->prep_p50_ms = pct_of(cp, 0.5); st->prep_p99_ms = pct_of(cp, 0.99);
+  st->start_p50_ms = pct_of(cs, 0.5); st->start_p99_ms = pct_of(cs, 0.99);
+  st->run_p50_ms = pct_of(cr, 0.5); st->run_p99_ms = pct_of(cr, 0.99);
+  st->gpu_p50_ms = pct_of(cg, 0.5); st->gpu_p99_ms = pct_of(cg, 0.99);
   return EA_OK;
 }
 

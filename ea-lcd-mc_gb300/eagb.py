@@ -57,7 +57,8 @@ class Request(C.Structure):
 
 class JobInfo(C.Structure):
     _fields_ = [("state", C.c_int32), ("bins_done", C.c_int32), ("t_submit", C.c_double), ("t_admit", C.c_double),
-                ("t_done", C.c_double), ("bytes", C.c_uint64), ("spin_updates", C.c_double)]
+                ("t_done", C.c_double), ("bytes", C.c_uint64), ("spin_updates", C.c_double),
+                ("t_ready", C.c_double), ("t_start", C.c_double), ("gpu_s", C.c_double)]
 
 
 class ServeStats(C.Structure):
@@ -65,7 +66,9 @@ class ServeStats(C.Structure):
                                           "bins", "batch_changes", "peak_running")] + \
                [(n, C.c_double) for n in ("p50_ms", "p99_ms", "mean_ms", "max_ms", "spin_updates", "span_s")] + \
                [(n, C.c_uint64) for n in ("budget", "bytes_in_use", "bytes_peak")] + \
-               [(n, C.c_double) for n in ("gpu_busy_s", "enqueue_s", "admit_s")]
+               [(n, C.c_double) for n in ("gpu_busy_s", "enqueue_s", "admit_s", "queue_p50_ms", "queue_p99_ms",
+                                          "prep_p50_ms", "prep_p99_ms", "start_p50_ms", "start_p99_ms",
+                                          "run_p50_ms", "run_p99_ms", "gpu_p50_ms", "gpu_p99_ms")]
 
 
 EA_JOB_QUEUED, EA_JOB_RUNNING, EA_JOB_DONE, EA_JOB_FAILED, EA_JOB_RELEASED = range(5)

@@ -436,6 +436,9 @@ typedef struct {
   double t_submit, t_admit, t_done;  /* seconds since the server's creation (-1: not yet) */
   uint64_t bytes;                    /* charged against the budget */
   double spin_updates;
+  double t_ready;   /* created and initialised by a preparation thread */
+  double t_start;   /* its first bin enqueued */
+  double gpu_s;     /* device time of the bins it took part in (a batch's bin counts for each member) */
 } ea_job_info;
 
 typedef struct {
@@ -448,6 +451,13 @@ typedef struct {
   double gpu_busy_s;  /* sum of the bins' device durations (CUDA events) */
   double enqueue_s;   /* worker time spent enqueueing bins (batch changes included) */
   double admit_s;     /* worker time spent creating and initialising admitted jobs */
+  /* Components of the completed jobs' latency, p50 / p99 in ms: queue wait
+   * (submission to admission by the HBM budget and the slots), preparation
+   * (admission to created and initialised), start wait (to the first bin
+   * enqueued) and run (first bin to completion); and the jobs' bin device
+   * time. */
+  double queue_p50_ms, queue_p99_ms, prep_p50_ms, prep_p99_ms, start_p50_ms, start_p99_ms;
+  double run_p50_ms, run_p99_ms, gpu_p50_ms, gpu_p99_ms;
 } ea_serve_stats;
 
 int ea_server_create(const ea_server_config *cfg, ea_server **out);

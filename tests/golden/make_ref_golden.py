@@ -50,7 +50,7 @@ CASES = {
     "r6_L24_Lz192_OBC_NB32": (24, 192, "OBC", 1, "T06_16_N32", 2, 2, None, 1, 1, 5, 1, 1, 0),
 }
 # timing runs of the reference binary (same geometry as bench.py): tag, nbits, nbin, itmax, houfr
-TIMING = {"t1_L24_Lz192_OBC_NB32_ns31": (31, 2, 20, 5)}
+TIMING = {"t1_L24_Lz192_OBC_NB32_ns31": (31, 3, 100, 5)}
 
 
 def case_inputs(tag, dirpath):

@@ -427,10 +427,13 @@ def oracle_bin(orc, itmax, houfr, mesfr, ptfr, cluster, nclust=0):
 # Lz=48, OBC, NT=24 in [0.7, 1.6], NR=4, 64 words (4096 samples), a bin of 10
 # sweeps with tempering after each and a Houdayer move on the colder half --
 # the 16-byte two-slot pass, the tile width, the energy chunking and the
-# 4-samples-per-pass labelling of 6912-site lattices as the bench runs them
+# 4-samples-per-pass labelling of 6912-site lattices as the bench runs them;
+# and the large tube as written (L=24, Lz=192, OBC, NT=32 in [0.6, 1.6],
+# NR=4, one word, a move every 5 sweeps): labelling in global scratch
 TIMED = [(6, 24, eagb.EA_PBC, "T08_16_N12", 2, 1, (512, 1, 1, 1, False)),
          (12, 48, eagb.EA_OBC, "T07_16_N24", 4, 1, (10, 10, 1, 1, True)),
-         (12, 48, eagb.EA_OBC, "T07_16_N24", 4, 64, (1, 10, 1, 1, True))]
+         (12, 48, eagb.EA_OBC, "T07_16_N24", 4, 64, (1, 10, 1, 1, True)),
+         (24, 192, eagb.EA_OBC, "T06_16_N32", 4, 1, (1, 5, 1, 1, True))]
 
 
 @pytest.mark.gpu
