@@ -651,6 +651,103 @@ def run_no_cluster(args, dev, torch, eagb):
             "l2": "flushed between steps (512 MB write)"}
 
 
+# many small sample-packed jobs: the serving configuration's distribution
+# (L in 6..20, Lz/L in {1,2,4,8,16}, PBC/OBC, NT in {8..32}, 64 samples, NR=4)
+# restricted to jobs of at most 2^20 spin words; one bin = 2 x (10 sweeps +
+# tempering each sweep + a Houdayer move) + measurements
+SPSMALL_WORKLOAD = "mixed_small_L6-20_LzL1-16_PBC-OBC_NT8-32_NR4_64samples_houfr10_%djobs"
+
+
+def spsmall_jobs(eagb, dev, njobs, seed=21):
+    rng = np.random.default_rng(seed)
+    specs = []
+    while len(specs) < njobs:
+        L = int(rng.integers(6, 21))
+        Lz = L * int(rng.choice([1, 2, 4, 8, 16]))
+        bc = int(rng.integers(0, 2))
+        nt = int(rng.choice(SERVE_NT))
+        if L * L * Lz * SERVE_NR * nt <= (1 << 20):
+            specs.append((L, Lz, bc, nt))
+    luts = {nt: np.load(os.path.join(ROOT, "tests", "golden", "lut_T07_16_N%d.npz" % nt)) for nt in SERVE_NT}
+    jobs = []
+    for k, (L, Lz, bc, nt) in enumerate(specs):
+        m = tuple((x ^ (0x9E3779B97F4A7C15 * (k + 1))) & 0xFFFFFFFFFFFFFFFF or 1 for x in MASTERS)
+        jobs.append(eagb.SpJob(L, Lz, luts[nt]["betas"], luts[nt]["cum"], nrep=SERVE_NR, nwords=1, bc=bc, seeds=m,
+                               jobid=k, device=dev))
+    return jobs
+
+
+def run_small_sp(args, dev, torch, eagb, njobs=64, steps=3):
+    """Sample-packed batching where jobs are small: plain (each job's bin a
+    graph on its own stream, all enqueued before waiting) vs batched (one
+    cooperative launch of the persistent bin kernel for every job), from twin
+    states; bit-exact check."""
+    plain, batched, graphed = (spsmall_jobs(eagb, dev, njobs), spsmall_jobs(eagb, dev, njobs),
+                               spsmall_jobs(eagb, dev, njobs))
+    batch = eagb.SpBatch(batched)
+    batch.set_bin_kernel(eagb.EA_BIN_PERSISTENT)
+    gbatch = eagb.SpBatch(graphed)
+    gbatch.set_bin_kernel(eagb.EA_BIN_GRAPH)
+    cad = dict(itmax=2, houfr=10, mesfr=1, ptfr=1, cluster=True)
+    su_step = sum(20 * j.V * SERVE_NR * j.g.nbetas * 64 for j in plain)
+    s0 = torch.cuda.Stream(device=dev)
+
+    def timed(streams_of, enqueue, n):
+        streams = [torch.cuda.ExternalStream(h, device=dev) for h in streams_of]
+        torch.cuda.synchronize(dev)
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(s0)
+        for st in streams:
+            st.wait_event(t0)
+        for _ in range(n):
+            enqueue()
+        for st in streams:
+            e = torch.cuda.Event()
+            e.record(st)
+            s0.wait_event(e)
+        t1.record(s0)
+        torch.cuda.synchronize(dev)
+        return t0.elapsed_time(t1)
+
+    def plain_step():
+        for j in plain:
+            j.run_async(**cad)
+
+    pstreams = [j.stream() for j in plain]
+    bstreams = [batch.stream()]
+    timed(pstreams, plain_step, 1)
+    gstreams = [gbatch.stream()]
+    timed(bstreams, lambda: batch.run_bin(**cad), 1)
+    timed(gstreams, lambda: gbatch.run_bin(**cad), 1)
+    batch.sync()
+    gbatch.sync()
+    ms_plain = timed(pstreams, plain_step, steps)
+    ms_batch = timed(bstreams, lambda: batch.run_bin(**cad), steps)
+    ms_graph = timed(gstreams, lambda: gbatch.run_bin(**cad), steps)
+    batch.sync()
+    gbatch.sync()
+    same = all(np.array_equal(a.get_spins(), b.get_spins()) and np.array_equal(a.get_spins(), c.get_spins())
+               for a, b, c in zip(plain, batched, graphed))
+    same = same and all(np.array_equal(a.bin_results(), b.bin_results()) for a, b in zip(plain, batched))
+    batch.close()
+    gbatch.close()
+    ms_seq = timed_sequential(torch, dev, plain, lambda j: j.run_async(**cad), 1)
+    for j in plain + batched + graphed:
+        j.close()
+    vp = su_step * steps / (ms_plain * 1e-3) / 1e12
+    vb = su_step * steps / (ms_batch * 1e-3) / 1e12
+    vs = su_step / (ms_seq * 1e-3) / 1e12
+    vg = su_step * steps / (ms_graph * 1e-3) / 1e12
+    return {"workload": SPSMALL_WORKLOAD % njobs, "jobs": njobs, "unit": "spin-updates/ps",
+            "plain_value": vp, "batched_value": vb, "speedup": vb / vp,
+            "batched_graph_value": vg, "speedup_graph": vg / vp,
+            "plain_sequential_value": vs, "speedup_vs_sequential": vb / vs,
+            "plain_ms_per_step": ms_plain / steps, "batched_ms_per_step": ms_batch / steps,
+            "spin_updates_per_step": su_step, "bit_exact_plain_vs_batched": bool(same),
+            "form": "batched = one cooperative launch of the persistent bin kernel per bin for every job; "
+                    "batched_graph = one graph launch per bin iteration, a branch per job"}
+
+
 def run_ours(args, rank, world, local):
     import torch
     eagb = load_eagb()
@@ -814,7 +911,8 @@ def run_ours(args, rank, world, local):
     line["no_cluster"] = run_no_cluster(args, dev, torch, eagb)
     if not args.no_mixed:
         line["batched"] = [run_mixed(args, dev, torch, eagb, 4, 8), run_mixed(args, dev, torch, eagb, 32, 1),
-                           run_mixed_sp(args, dev, torch, eagb), run_mixed_sp(args, dev, torch, eagb, 72, 10)]
+                           run_mixed_sp(args, dev, torch, eagb), run_mixed_sp(args, dev, torch, eagb, 72, 10),
+                           run_small_sp(args, dev, torch, eagb)]
     if not args.no_serve:
         line["serving"] = run_serve(args, dev, eagb)
         line["serving_sample_packed"] = run_serve_sp(args, dev, eagb)
@@ -845,6 +943,8 @@ def main():
                     help="only two bins of the 36-job x 32-sample multispin mix in this form (for profilers)")
     ap.add_argument("--rng-sms", type=int, default=-1,
                     help="SMs of the cluster-uniform generator's partition for the headline job (-1: automatic)")
+    ap.add_argument("--small-sp", type=int, default=0, metavar="N",
+                    help="only the small sample-packed batching leg with N jobs (prints its record)")
     ap.add_argument("--serve-config5", type=int, default=0, metavar="N",
                     help="only the serving configuration at its stated size: N jobs drawn from it (prints its record)")
     ap.add_argument("--sp-case", default="", help="run only the sample-packed workloads whose name contains this "
@@ -876,6 +976,9 @@ def main():
                 j.sync()
         for j in jobs:
             j.close()
+    elif args.small_sp:
+        import torch
+        print(json.dumps(run_small_sp(args, local, torch, load_eagb(), args.small_sp)), flush=True)
     elif args.serve_config5:
         print(json.dumps(run_serve_c5(args, local, load_eagb(), args.serve_config5)), flush=True)
     elif args.sp_case:

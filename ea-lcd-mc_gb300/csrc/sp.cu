@@ -1537,17 +1537,13 @@ int ea_sp_houdayer(ea_sp *c, int32_t nclust) {
   return sp_houdayer(c, nclust);
 }
 
-// Batches whose jobs all have at most this many spin words run their bins in
-// the persistent kernel under EA_BIN_AUTO.  A job alone takes the graph: each
-// phase of a small job is a latency-bound chain that a barrier does not
-// shorten, and the graph's per-phase kernels run at twice the persistent
-// kernel's occupancy (measured: 84 vs 106 us per sweep at L=6, Lz=24, NT=12).
-constexpr double kSpPersistMaxWords = 1048576.0;
-
-static bool sp_small(const SpDev &d) {
-  return (double)d.nw * d.V * d.NR * d.NB <= kSpPersistMaxWords && d.ncol <= kSpBatchMaxColours;
-}
-
+// EA_BIN_AUTO takes the graph.  Measured on GB300: a job alone, each phase of
+// a small job is a latency-bound chain that a barrier does not shorten, and
+// the graph's per-phase kernels run at twice the persistent kernel's
+// occupancy (84 vs 106 us per sweep at L=6, Lz=24, NT=12); 64 small jobs of
+// the serving mix, the phases in lock-step wait for each phase's slowest
+// job, while the jobs' graphs on their own streams interleave (0.20 vs 0.42
+// spin-updates/ps).
 static bool sp_use_persist(int mode, const SpDev &) { return mode == EA_BIN_PERSISTENT; }
 
 // The work list of the job alone (its blocks of every kind, as a batch of
@@ -1872,11 +1868,7 @@ int ea_sp_batch_run(ea_sp_batch *b, const ea_cadence *cad) {
     SCU(cudaEventRecord(b->done, c->st));
     SCU(cudaStreamWaitEvent(b->bs, b->done, 0));
   }
-  bool persist = b->bin_mode == EA_BIN_PERSISTENT;
-  if (b->bin_mode == EA_BIN_AUTO) {
-    persist = b->jobs.size() > 1;
-    for (ea_sp *c : b->jobs) persist = persist && sp_small(c->d);
-  }
+  const bool persist = b->bin_mode == EA_BIN_PERSISTENT;
   if (persist) {
     // one work list of every job, one cooperative launch per bin
     if ((rc = spb_upload(b->all, cad->cluster != 0, b->bs))) return rc;

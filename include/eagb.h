@@ -361,9 +361,9 @@ int ea_sp_bin_results(ea_sp *job, double *avgE);
  * are identical; it removes the per-phase launch gaps that bound jobs too
  * small to fill the GPU.  A barrier wait gives up after 4 s (the kernel
  * returns) and the next ea_sp_sync / ea_sp_bin_results / ea_sp_batch_sync
- * reports EA_ERR_CUDA.  EA_BIN_AUTO (default): a job alone takes the graph;
- * a batch of two or more jobs takes the persistent kernel when every job has
- * at most 2^20 spin words (nwords x V x NR x NB), the graph otherwise. */
+ * reports EA_ERR_CUDA.  EA_BIN_AUTO (default): the graph, which measured
+ * faster on GB300 for a small job alone and for batches of small jobs (a
+ * batch's phases in lock-step wait for each phase's slowest job). */
 enum { EA_BIN_AUTO = 0, EA_BIN_GRAPH = 1, EA_BIN_PERSISTENT = 2 };
 int ea_sp_set_bin_kernel(ea_sp *job, int32_t mode);
 /* Batches of sample-packed jobs (any geometries, replica and temperature
