@@ -165,13 +165,15 @@ constexpr int kSpChunkMax = 256;  // sites per thread: 6 * 256 < 2^11
 constexpr int kSpPlanes = 11;
 
 // Sites per thread of the energy kernel: enough threads to fill the GPU
-// (152 SMs x 2048), at least 16 sites each (each thread ends with 64 atomic
-// additions, which small chunks pile on the same counters; larger chunks
-// leave small jobs with too few threads -- 8 and 32 measured either side).
+// (152 SMs x 2048), at least 4 sites each (each thread ends with up to 64
+// atomic additions, which small chunks pile on the same counters).  Jobs too
+// small to fill the GPU get the floor: their count is a chain of dependent
+// loads per site, so fewer sites a thread is a shorter chain (16 sites a
+// thread measured 16-21 us per count on one-word jobs).
 int sp_energy_chunk(const SpDev &d) {
   const double words = (double)d.nw * d.V * d.NR * d.NB;
   int c = (int)(words / (152.0 * 2048.0));
-  return c < 16 ? 16 : (c > kSpChunkMax ? kSpChunkMax : c);
+  return c < 4 ? 4 : (c > kSpChunkMax ? kSpChunkMax : c);
 }
 
 // col: the thread's index over nw * nchunk * G (blocks of 256 threads).
@@ -243,16 +245,19 @@ __device__ __forceinline__ void sp_pt_body(const SpDev &d, int wr, int lane) {
   const unsigned long long step = *d.ptstep;
   const uint32_t chain = (uint32_t)(((size_t)w * 64 + lane) * NR + r);
   const double FNORM = 5.4210108624275218e-20;
-  int E[64];
-  uint8_t pm[64];
-  for (int b = 0; b < NB; ++b) {
-    E[b] = nt - d.U2[o + b];
-    pm[b] = d.perm[o + b];
-  }
   uint32_t *acc = d.acc + ((size_t)w * 64 + lane) * NR * (NB - 1) + (size_t)r * (NB - 1);
   uint32_t *Mh = reinterpret_cast<uint32_t *>(d.M + ((size_t)w * NR + r) * (NB - 1));
+  // The pairs in order: slot i+1 still holds its own configuration when pair
+  // i is decided, slot i holds the one carried up from below (a swap at i
+  // moves it on to i+1).  So the chain keeps only the carried energy and id
+  // in registers; slot i's final values are written as soon as pair i is
+  // decided.
+  int carry_e = nt - d.U2[o];
+  uint8_t carry_p = d.perm[o];
   for (int i = 0; i < NB - 1; ++i) {
-    const int dE = E[i + 1] - E[i];
+    const int e1 = nt - d.U2[o + i + 1];
+    const uint8_t p1 = d.perm[o + i + 1];
+    const int dE = e1 - carry_e;
     const double pt = __dmul_rn(-__dsub_rn(d.betas[i + 1], d.betas[i]), (double)dE);
     uint32_t v0 = (uint32_t)step, v1 = (uint32_t)(step >> 32), v2 = (uint32_t)i, v3 = chain;
     philox10(v0, v1, v2, v3, (uint32_t)d.pt_seed, (uint32_t)(d.pt_seed >> 32));
@@ -265,17 +270,20 @@ __device__ __forceinline__ void sp_pt_body(const SpDev &d, int wr, int lane) {
       change = (m >= 1 && m <= nx) ? __dmul_rn(FNORM, __ull2double_rn(u)) < d.exptab[base + m - 1] : u == 0;
     }
     if (change) {
-      const int te = E[i]; E[i] = E[i + 1]; E[i + 1] = te;
-      const uint8_t tp = pm[i]; pm[i] = pm[i + 1]; pm[i + 1] = tp;
+      d.E[o + i] = e1;
+      d.perm[o + i] = p1;
       acc[i] += 1u;
+    } else {
+      d.E[o + i] = carry_e;
+      d.perm[o + i] = carry_p;
+      carry_e = e1;
+      carry_p = p1;
     }
     const unsigned mask = __ballot_sync(0xffffffffu, change);
     if ((lane & 31) == 0) Mh[2 * i + (lane >> 5)] = mask;
   }
-  for (int b = 0; b < NB; ++b) {
-    d.E[o + b] = E[b];
-    d.perm[o + b] = pm[b];
-  }
+  d.E[o + NB - 1] = carry_e;
+  d.perm[o + NB - 1] = carry_p;
 }
 
 // The accepted swaps of the last tempering step, applied to the words in
