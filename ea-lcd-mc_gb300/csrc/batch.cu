@@ -67,7 +67,7 @@ __global__ void kb_fill_bits(const __grid_constant__ BatchDev b, int parity) {
 }
 
 template <int NR, int KT, bool UPDATE>
-__global__ void __launch_bounds__(512) kb_sweep(const __grid_constant__ BatchDev b, int parity, int energy) {
+__global__ void __launch_bounds__(512, 2) kb_sweep(const __grid_constant__ BatchDev b, int parity, int energy) {
   extern __shared__ __align__(16) unsigned char smem[];
   int staged = -1;  // job whose thresholds are in SMEM
   BATCH_LOOP(KB_SWEEP) {

@@ -26,7 +26,7 @@ void set_dividers(JobDev &j) {
 __global__ void k_fill_bits(const __grid_constant__ JobDev j, int parity) { fill_bits_body(j, parity); }
 
 template <int NR, int KT, bool UPDATE>
-__global__ void __launch_bounds__(512, 3) k_sweep(const __grid_constant__ JobDev j, int parity, int energy) {
+__global__ void __launch_bounds__(512, 2) k_sweep(const __grid_constant__ JobDev j, int parity, int energy) {
   extern __shared__ __align__(16) unsigned char smem[];
   sweep_body<NR, KT, UPDATE>(j, blockIdx.x, parity, energy, smem);
 }

@@ -212,9 +212,11 @@ __device__ __forceinline__ void sweep_body(const JobDev &j, int tile, int parity
   }
 
   // Update phase.  Lanes form groups of G = KT*NR; a lane keeps its
-  // (half-site, replica) and its neighbour record for the whole loop and walks
-  // the (sample, clone) pairs with a stride of one group per iteration, so the
-  // G lanes of a group touch G consecutive words of one clone array.
+  // (half-site, replica) and its neighbour record for the whole loop, and a
+  // group walks a contiguous run of (sample, clone) pairs, clone fastest, so
+  // the G lanes of a group touch G consecutive words of one clone array and a
+  // lane loads the six coupling words of its (sample, half-site) once per
+  // sample rather than once per word.
   constexpr int G = KT * NR;
   const size_t wpc = (size_t)half * NR, wpp = wpc * NB;
   const int lg = tid % G, grp = tid / G, ngrp = nth / G;
@@ -226,22 +228,28 @@ __device__ __forceinline__ void sweep_body(const JobDev &j, int tile, int parity
   for (int d = 0; d < 6; ++d) nb[d] = s_nb[kk * 8 + d];
   const int nflags = s_nb[kk * 8 + 6];
   const int nsc = j.ns * NB, iters = (nsc + ngrp - 1) / ngrp;
-  const int ds = ngrp / NB, dc = ngrp % NB;
-  int s = grp / NB, c = grp % NB;
-  for (int it = 0, sc = grp; it < iters; ++it, sc += ngrp) {
+  const int sc0 = grp * iters;
+  int s = sc0 / NB, c = sc0 - s * NB, js = -1;
+  u64 jw[6];
+  for (int it = 0, sc = sc0; it < iters; ++it, ++sc) {
     const bool valid = kvalid && sc < nsc;
     int e = 0;
     if (valid) {
       u64 *base = j.spins + (size_t)s * 2 * wpp + (size_t)c * wpc;
       u64 *tgt = base + (size_t)parity * wpp + (size_t)k * NR + r;
       const u64 *oth = base + (size_t)(1 - parity) * wpp + r;
-      const u64 *Jp = j.J + ((size_t)s * 2 + parity) * 6 * half + k;
+      if (s != js) {
+        const u64 *Jp = j.J + ((size_t)s * 2 + parity) * 6 * half + k;
+#pragma unroll
+        for (int d = 0; d < 6; ++d) jw[d] = __ldg(Jp + (size_t)d * half);
+        js = s;
+      }
       const u64 sv = *tgt;
       u64 n[6];
       gather6(oth, nb, nflags, parity, obc, NR, n);
       u64 f[6];
 #pragma unroll
-      for (int d = 0; d < 6; ++d) f[d] = sv ^ __ldg(Jp + (size_t)d * half) ^ n[d];
+      for (int d = 0; d < 6; ++d) f[d] = sv ^ jw[d] ^ n[d];
       u64 fl = 0;
       if (UPDATE) {
         const int beta = j.wbtc[(s * NR + r) * NB + c];
@@ -261,8 +269,7 @@ __device__ __forceinline__ void sweep_body(const JobDev &j, int tile, int parity
       for (int m = NR; m < G; m <<= 1) e += __shfl_xor_sync(0xffffffffu, e, m);
       if (valid && kk == 0) j.epart[(((size_t)tile * j.ns + s) * NB + c) * NR + r] = e;
     }
-    c += dc; s += ds;
-    if (c >= NB) { c -= NB; ++s; }
+    if (++c == NB) { c = 0; ++s; }
   }
 }
 
