@@ -571,8 +571,11 @@ __device__ __forceinline__ void sp_flip_body(const SpDev &d, int g, long long t)
 }
 
 // Energy measurement of a bin's iteration: avgE += 3V - U2 (slot order).
-__device__ __forceinline__ void sp_measure_u2_body(const SpDev &d, long long i) {
-  if (i < (long long)d.nw * 64 * d.NR * d.NB) d.avgE[i] += (double)(3 * d.V - d.U2[i]);
+// from_e: the measurement follows a tempering step directly (no cluster
+// move in between), whose E already holds the energy of the configuration
+// now at each slot (energies move with their configurations): no recount.
+__device__ __forceinline__ void sp_measure_u2_body(const SpDev &d, long long i, int from_e) {
+  if (i < (long long)d.nw * 64 * d.NR * d.NB) d.avgE[i] += from_e ? (double)d.E[i] : (double)(3 * d.V - d.U2[i]);
 }
 
 // ---------------------------------------------------------------------------
@@ -704,9 +707,9 @@ __global__ void __launch_bounds__(kPermRows) kb_sp_permute(const __grid_constant
   SPB_ITEM(SPB_PERMUTE)
   sp_permute_body(d, blk, rows);
 }
-__global__ void kb_sp_measure(const __grid_constant__ SpBatchDev b) {
+__global__ void kb_sp_measure(const __grid_constant__ SpBatchDev b, int from_e) {
   SPB_ITEM(SPB_MEASURE)
-  sp_measure_u2_body(d, (long long)blk * blockDim.x + threadIdx.x);
+  sp_measure_u2_body(d, (long long)blk * blockDim.x + threadIdx.x, from_e);
 }
 __global__ void kb_sp_pairs(const __grid_constant__ SpBatchDev b) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -797,9 +800,9 @@ cudaError_t sp_batch_houdayer(const SpBatchDev &b, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-cudaError_t sp_batch_measure(const SpBatchDev &b, cudaStream_t st) {
-  spb_energy(b, st);
-  kb_sp_measure<<<b.total[SPB_MEASURE], 256, 0, st>>>(b);
+cudaError_t sp_batch_measure(const SpBatchDev &b, bool from_e, cudaStream_t st) {
+  if (!from_e) spb_energy(b, st);
+  kb_sp_measure<<<b.total[SPB_MEASURE], 256, 0, st>>>(b, from_e ? 1 : 0);
   return cudaGetLastError();
 }
 
@@ -947,8 +950,8 @@ __global__ void __launch_bounds__(kPersistThreads, 1) k_sp_persist(const __grid_
         }
       }
     }
-    if (!energy()) return;
-    SPP_SUB(SPB_MEASURE, 256, sp_measure_u2_body(d, (long long)blk * 256 + ltid))
+    if (p.cluster && !energy()) return;
+    SPP_SUB(SPB_MEASURE, 256, sp_measure_u2_body(d, (long long)blk * 256 + ltid, !p.cluster))
     SPP_SYNC();
   }
 }
@@ -1015,8 +1018,8 @@ __global__ void __launch_bounds__(1024) k_sp_cluster(const __grid_constant__ SpD
 __global__ void k_sp_flip(const __grid_constant__ SpDev d, int g) {
   sp_flip_body(d, g, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
-__global__ void k_sp_measure_u2(const __grid_constant__ SpDev d) {
-  sp_measure_u2_body(d, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+__global__ void k_sp_measure_u2(const __grid_constant__ SpDev d, int from_e) {
+  sp_measure_u2_body(d, (long long)blockIdx.x * blockDim.x + threadIdx.x, from_e);
 }
 
 // ---------------------------------------------------------------------------
@@ -1105,9 +1108,9 @@ cudaError_t sp_launch_houdayer(const SpDev &d, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-cudaError_t sp_launch_measure_u2(const SpDev &d, cudaStream_t st) {
+cudaError_t sp_launch_measure_u2(const SpDev &d, bool from_e, cudaStream_t st) {
   const long long n = (long long)d.nw * 64 * d.NR * d.NB;
-  k_sp_measure_u2<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d);
+  k_sp_measure_u2<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d, from_e ? 1 : 0);
   return cudaGetLastError();
 }
 
@@ -1621,8 +1624,9 @@ int ea_sp_run(ea_sp *c, const ea_cadence *cad, double *avgE) {
       }
       if (cad->cluster) SCU(sp_launch_houdayer(c->d, c->st));
     }
-    SCU(sp_launch_energy(c->d, c->st));
-    SCU(sp_launch_measure_u2(c->d, c->st));
+    // without cluster moves the last tempering step's energies are current
+    if (cad->cluster) SCU(sp_launch_energy(c->d, c->st));
+    SCU(sp_launch_measure_u2(c->d, !cad->cluster, c->st));
     return EA_OK;
   };
   if (cad->itmax == 1) {
@@ -1758,7 +1762,7 @@ static cudaError_t spb_iteration(const SpClass &k, const ea_cadence *cad, cudaSt
     }
     if (e == cudaSuccess && cad->cluster) e = sp_batch_houdayer(k.bd, st);
   }
-  if (e == cudaSuccess) e = sp_batch_measure(k.bd, st);
+  if (e == cudaSuccess) e = sp_batch_measure(k.bd, !cad->cluster, st);
   return e;
 }
 

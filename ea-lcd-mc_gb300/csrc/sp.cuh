@@ -92,7 +92,7 @@ cudaError_t sp_launch_energy(const SpDev &d, cudaStream_t st);
 cudaError_t sp_launch_pt(const SpDev &d, cudaStream_t st);
 cudaError_t sp_launch_permute(const SpDev &d, cudaStream_t st);
 cudaError_t sp_launch_houdayer(const SpDev &d, cudaStream_t st);
-cudaError_t sp_launch_measure_u2(const SpDev &d, cudaStream_t st);
+cudaError_t sp_launch_measure_u2(const SpDev &d, bool from_e, cudaStream_t st);
 cudaError_t sp_launch_dos(const SpDev &d, cudaStream_t st);
 cudaError_t sp_launch_exact(const SpDev &d, const double *betas, int nbeta, double *meanE, cudaStream_t st);
 
@@ -129,6 +129,6 @@ cudaError_t sp_batch_setup();
 cudaError_t sp_batch_sweep(const SpBatchDev &b, int ncol_max, cudaStream_t st);
 cudaError_t sp_batch_tempering(const SpBatchDev &b, cudaStream_t st);
 cudaError_t sp_batch_houdayer(const SpBatchDev &b, cudaStream_t st);
-cudaError_t sp_batch_measure(const SpBatchDev &b, cudaStream_t st);
+cudaError_t sp_batch_measure(const SpBatchDev &b, bool from_e, cudaStream_t st);
 
 }  // namespace eagb
