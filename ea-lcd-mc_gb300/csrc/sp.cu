@@ -557,6 +557,133 @@ __device__ __forceinline__ void sp_cluster4_body(const SpDev &d, int g, int blk,
   for (int i = threadIdx.x; i < V; i += blockDim.x) Qb[(size_t)i * 8] = fb[i];
 }
 
+// The same labelling for all 8 samples of the CTA at once, for lattices up
+// to kSpCluster8MaxV sites: 16-bit labels, a site's 8 in one 16-byte SMEM
+// slot, its 8 bond masks in one 64-bit word (sample l at bits 8l..8l+5), so
+// one neighbour-table load and one loop step serve the 8 samples, in a single
+// pass (26 bytes of SMEM per site).  SMEM has no 16-bit atomicMin, so a hook
+// is a plain store: when several threads hook one root in a round, one
+// store stays and the other bonds are hooked again in the next round, as
+// with atomicMin (which keeps one link per root and round as well).  Every
+// value stored is a smaller site of the same cluster, so labels still end at
+// each cluster's smallest site.
+constexpr int kSpCluster8MaxV = 8900;
+
+__device__ __forceinline__ unsigned long long spread8(uint32_t x) {
+  unsigned long long r = 0;
+#pragma unroll
+  for (int l = 0; l < 8; ++l) r |= (unsigned long long)((x >> l) & 1u) << (8 * l);
+  return r;
+}
+
+__device__ __forceinline__ void unpack8(uint4 v, uint32_t l[8]) {
+  l[0] = v.x & 0xFFFFu; l[1] = v.x >> 16; l[2] = v.y & 0xFFFFu; l[3] = v.y >> 16;
+  l[4] = v.z & 0xFFFFu; l[5] = v.z >> 16; l[6] = v.w & 0xFFFFu; l[7] = v.w >> 16;
+}
+
+__device__ __forceinline__ uint4 pack8(const uint32_t l[8]) {
+  return make_uint4(l[0] | (l[1] << 16), l[2] | (l[3] << 16), l[4] | (l[5] << 16), l[6] | (l[7] << 16));
+}
+
+__device__ __forceinline__ void sp_cluster8_body(const SpDev &d, int g, int blk, unsigned char *sm) {
+  const unsigned long long key = sp_cluster_key(d);
+  const int V = d.V, nc = d.nclust;
+  uint4 *lab = reinterpret_cast<uint4 *>(sm);                                  // [V]: 8 labels
+  uint16_t *lab16 = reinterpret_cast<uint16_t *>(sm);                          // the same, one label each
+  unsigned long long *bond = reinterpret_cast<unsigned long long *>(sm + (size_t)16 * V);  // [V]
+  uint8_t *qb = sm + (size_t)24 * V;                                           // [V] q bits, then coins
+  const int grp = blk & 7, lat = blk >> 3;
+  const int b = lat % nc, w = lat / nc;
+  uint8_t *Qb = reinterpret_cast<uint8_t *>(d.Q + (size_t)lat * V) + grp;
+  for (int i = threadIdx.x; i < V; i += blockDim.x) qb[i] = Qb[(size_t)i * 8];
+  __syncthreads();
+  for (int i = threadIdx.x; i < V; i += blockDim.x) {
+    const uint32_t qi = qb[i];
+    unsigned long long m = 0;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+      const int p = __ldg(d.nb + (size_t)i * 6 + q);
+      if (p < i) m |= spread8(~(qi ^ qb[p]) & 0xFFu) << q;
+    }
+    bond[i] = m;
+    const uint32_t ii = (uint32_t)i | ((uint32_t)i << 16);
+    lab[i] = make_uint4(ii, ii, ii, ii);
+  }
+  __syncthreads();
+  for (;;) {
+    int hooked = 0;
+    for (int i = threadIdx.x; i < V; i += blockDim.x) {
+      const unsigned long long m = bond[i];
+      if (!m) continue;
+      uint32_t li[8];
+      unpack8(lab[i], li);
+#pragma unroll
+      for (int q = 0; q < 6; ++q) {
+        const unsigned long long mq = (m >> q) & 0x0101010101010101ull;
+        if (!mq) continue;
+        const int p = __ldg(d.nb + (size_t)i * 6 + q);
+        uint32_t lj[8];
+        unpack8(lab[p], lj);
+#pragma unroll
+        for (int l = 0; l < 8; ++l)
+          if (((mq >> (8 * l)) & 1ull) && lj[l] != li[l]) {
+            lab16[8 * (size_t)max(li[l], lj[l]) + l] = (uint16_t)min(li[l], lj[l]);
+            hooked = 1;
+          }
+      }
+    }
+    if (!__syncthreads_or(hooked)) break;
+    for (;;) {
+      int moved = 0;
+      for (int i = threadIdx.x; i < V; i += blockDim.x) {
+        uint32_t x[8], y[8];
+        unpack8(lab[i], x);
+        bool ch = false;
+#pragma unroll
+        for (int l = 0; l < 8; ++l) {
+          y[l] = lab16[8 * (size_t)x[l] + l];
+          ch |= y[l] != x[l];
+        }
+        if (ch) { lab[i] = pack8(y); moved = 1; }
+      }
+      if (!__syncthreads_or(moved)) break;
+    }
+  }
+  // coins of the roots (in qb, no longer needed), then the flip bytes
+  const unsigned long long mv = *d.move;
+  for (int i = threadIdx.x; i < V; i += blockDim.x) {
+    uint32_t x[8];
+    unpack8(lab[i], x);
+    uint32_t c = 0;
+#pragma unroll
+    for (int l = 0; l < 8; ++l) {
+      if (x[l] != (uint32_t)i) continue;
+      const int lane = grp * 8 + l;
+      const uint32_t tag = (((uint32_t)(w * 64 + lane) << 6 | (uint32_t)b) << 1) | (uint32_t)g;
+      uint32_t v0 = (uint32_t)mv, v1 = (uint32_t)(mv >> 32), v2 = (uint32_t)i, v3 = tag;
+      philox10(v0, v1, v2, v3, (uint32_t)key, (uint32_t)(key >> 32));
+      c |= (v0 & 1u) << l;
+    }
+    qb[i] = (uint8_t)c;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < V; i += blockDim.x) {
+    uint32_t x[8];
+    unpack8(lab[i], x);
+    uint32_t f = 0;
+#pragma unroll
+    for (int l = 0; l < 8; ++l) f |= ((uint32_t)(qb[x[l]] >> l) & 1u) << l;
+    Qb[(size_t)i * 8] = (uint8_t)f;
+  }
+}
+
+// Labelling of one CTA's (word, slot, 8 samples) by lattice size.
+__device__ __forceinline__ void sp_cluster_any(const SpDev &d, int g, int blk, unsigned char *sm) {
+  if (d.V <= kSpCluster8MaxV) sp_cluster8_body(d, g, blk, sm);
+  else if (d.V <= kSpCluster4MaxV) sp_cluster4_body(d, g, blk, reinterpret_cast<uint32_t *>(sm));
+  else sp_cluster_body(d, g, blk, reinterpret_cast<uint32_t *>(sm));
+}
+
 // Both replicas of the group take the flip words: thread per (word, site, slot).
 __device__ __forceinline__ void sp_flip_body(const SpDev &d, int g, long long t) {
   const int V = d.V, nc = d.nclust;
@@ -719,11 +846,10 @@ __global__ void kb_sp_overlap(const __grid_constant__ SpBatchDev b, int g) {
   SPB_ITEM(SPB_OVL0 + g)
   sp_overlap_body(d, g, (long long)blk * blockDim.x + threadIdx.x);
 }
-__global__ void __launch_bounds__(1024) kb_sp_cluster(const __grid_constant__ SpBatchDev b, int g) {
+__global__ void __launch_bounds__(1024, 1) kb_sp_cluster(const __grid_constant__ SpBatchDev b, int g) {
   extern __shared__ __align__(16) uint32_t sm[];
   SPB_ITEM(SPB_CL0 + g)
-  if (d.V <= kSpCluster4MaxV) sp_cluster4_body(d, g, blk, sm);
-  else sp_cluster_body(d, g, blk, sm);
+  sp_cluster_any(d, g, blk, reinterpret_cast<unsigned char *>(sm));
 }
 __global__ void kb_sp_flip(const __grid_constant__ SpBatchDev b, int g) {
   SPB_ITEM(SPB_FL0 + g)
@@ -940,10 +1066,7 @@ __global__ void __launch_bounds__(kPersistThreads, 1) k_sp_persist(const __grid_
           if (!b.total[SPB_CL0 + g]) continue;
           SPP_SUB(SPB_OVL0 + g, 256, sp_overlap_body(d, g, (long long)blk * 256 + ltid))
           SPP_SYNC();
-          SPP_BLOCKS(SPB_CL0 + g, {
-            if (d.V <= kSpCluster4MaxV) sp_cluster4_body(d, g, blk, reinterpret_cast<uint32_t *>(smem));
-            else sp_cluster_body(d, g, blk, reinterpret_cast<uint32_t *>(smem));
-          })
+          SPP_BLOCKS(SPB_CL0 + g, sp_cluster_any(d, g, blk, smem))
           SPP_SYNC();
           SPP_SUB(SPB_FL0 + g, 256, sp_flip_body(d, g, (long long)blk * 256 + ltid))
           SPP_SYNC();
@@ -1010,10 +1133,9 @@ __global__ void k_sp_pairs(const __grid_constant__ SpDev d) {
 __global__ void k_sp_overlap(const __grid_constant__ SpDev d, int g) {
   sp_overlap_body(d, g, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
-__global__ void __launch_bounds__(1024) k_sp_cluster(const __grid_constant__ SpDev d, int g) {
+__global__ void __launch_bounds__(1024, 1) k_sp_cluster(const __grid_constant__ SpDev d, int g) {
   extern __shared__ __align__(16) uint32_t sm[];
-  if (d.V <= kSpCluster4MaxV) sp_cluster4_body(d, g, blockIdx.x, sm);
-  else sp_cluster_body(d, g, blockIdx.x, sm);
+  sp_cluster_any(d, g, blockIdx.x, reinterpret_cast<unsigned char *>(sm));
 }
 __global__ void k_sp_flip(const __grid_constant__ SpDev d, int g) {
   sp_flip_body(d, g, (long long)blockIdx.x * blockDim.x + threadIdx.x);
@@ -1050,7 +1172,8 @@ cudaError_t sp_setup() {
   cudaError_t e = cudaFuncSetAttribute(k_sp_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_sp_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)std::max(sp_cluster_smem(kSpClusterMaxV), sp_cluster_smem(kSpCluster4MaxV)));
+                             (int)std::max(sp_cluster_smem(kSpClusterMaxV),
+                                           std::max(sp_cluster_smem(kSpCluster4MaxV), sp_cluster_smem(kSpCluster8MaxV))));
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_sp_permute, cudaFuncAttributeMaxDynamicSharedMemorySize, kPermRows * 65 * 8);
   return e;
@@ -1088,7 +1211,7 @@ cudaError_t sp_launch_permute(const SpDev &d, cudaStream_t st) {
 
 
 size_t sp_cluster_smem(int V) {
-  return V <= kSpCluster4MaxV ? (size_t)V * 22 : V <= kSpClusterMaxV ? (size_t)V * 7 : 0;
+  return V <= kSpCluster8MaxV ? (size_t)V * 26 : V <= kSpCluster4MaxV ? (size_t)V * 22 : V <= kSpClusterMaxV ? (size_t)V * 7 : 0;
 }
 
 // Block size of the cluster labelling: 1024 threads, 256 for lattices of
