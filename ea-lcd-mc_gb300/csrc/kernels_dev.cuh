@@ -32,28 +32,31 @@ __device__ __forceinline__ u64 d_hq_next(ea_hq *h) {
   return h->final;
 }
 
+// One step of a replica's two generators and the counter it gives for time
+// counter `iter` (the state may live in global or shared memory).
+__device__ __forceinline__ uint4 next_counter(ea_xoshiro *x, ea_hq *h, long long iter, int parity, uint32_t jobid) {
+  u64 s0 = x->s[0], s1 = x->s[1], s2 = x->s[2], s3 = x->s[3];
+  const u64 xf = d_rotl(s0 + s3, 23) + s0;
+  const u64 t = s1 << 17;
+  s2 ^= s0; s3 ^= s1; s1 ^= s2; s0 ^= s3; s2 ^= t; s3 = d_rotl(s3, 45);
+  x->s[0] = s0; x->s[1] = s1; x->s[2] = s2; x->s[3] = s3; x->t = t; x->final = xf;
+  const u64 pf = d_hq_next(h);
+  u64 e = (pf + xf) >> 12;
+  uint4 c;
+  c.y = (uint32_t)((u64)iter >> 15);
+  c.x = (uint32_t)((((u64)iter & 32767ULL) << 3) | ((u64)(parity & 1) << 2));
+  c.x |= (uint32_t)((e & 0x3FFFULL) << 18); e >>= 14;
+  c.y |= (uint32_t)((e & 0x7FULL) << 25); e >>= 7;
+  c.z = (uint32_t)((e & 0x1FFFULL) << 19); e >>= 13;
+  c.w = ((uint32_t)(e << 14)) | jobid;
+  return c;
+}
+
 __device__ __forceinline__ void fill_bits_body(const JobDev &j, int parity) {
   const int r = threadIdx.x;
   const long long iter = *j.iter;
   __syncthreads();
-  if (r < j.NR) {
-    ea_xoshiro *x = j.xo + r;
-    u64 s0 = x->s[0], s1 = x->s[1], s2 = x->s[2], s3 = x->s[3];
-    const u64 xf = d_rotl(s0 + s3, 23) + s0;
-    const u64 t = s1 << 17;
-    s2 ^= s0; s3 ^= s1; s1 ^= s2; s0 ^= s3; s2 ^= t; s3 = d_rotl(s3, 45);
-    x->s[0] = s0; x->s[1] = s1; x->s[2] = s2; x->s[3] = s3; x->t = t; x->final = xf;
-    const u64 pf = d_hq_next(j.prc + r);
-    u64 e = (pf + xf) >> 12;
-    uint4 c;
-    c.y = (uint32_t)((u64)iter >> 15);
-    c.x = (uint32_t)((((u64)iter & 32767ULL) << 3) | ((u64)(parity & 1) << 2));
-    c.x |= (uint32_t)((e & 0x3FFFULL) << 18); e >>= 14;
-    c.y |= (uint32_t)((e & 0x7FULL) << 25); e >>= 7;
-    c.z = (uint32_t)((e & 0x1FFFULL) << 19); e >>= 13;
-    c.w = ((uint32_t)(e << 14)) | j.jobid;
-    j.ctr[r] = c;
-  }
+  if (r < j.NR) j.ctr[r] = next_counter(j.xo + r, j.prc + r, iter, parity, j.jobid);
   if (r == 0) *j.iter = iter + 1;
 }
 

@@ -1300,6 +1300,15 @@ struct ea_sp {
   int *p_err = nullptr;
   SpDev p_up{};                       // descriptor last uploaded
   bool p_valid = false;
+  // resident bin kernel (EA_BIN_RESIDENT): plan for the descriptor r_dev,
+  // Philox counters and random words of one launch's passes
+  SpResPlan r_plan{};
+  SpDev r_dev{};
+  int r_state = 0;                    // 0: not planned, 1: eligible, 2: not eligible
+  uint4 *r_ctrs = nullptr;
+  unsigned long long *r_R = nullptr, *r_X = nullptr;
+  size_t r_cap_pass = 0, r_cap_sweep = 0, r_cap_pt = 0;
+  bool pair_energy = false;           // see sp_pair_energy
 };
 
 namespace {
@@ -1361,6 +1370,7 @@ int ea_sp_create(const ea_sp_geom *gp, int32_t device, ea_sp **out) {
   cudaError_t e = cudaSetDevice(device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = sp_setup();
+  if (e == cudaSuccess) e = sp_res_setup();
   if (e != cudaSuccess) { delete c; return spfail(EA_ERR_CUDA, "set-up: %s", cudaGetErrorString(e)); }
   const size_t G = (size_t)d.NR * d.NB, V = g.V, nw = d.nw;
   int rc;
@@ -1414,6 +1424,9 @@ int ea_sp_destroy(ea_sp *c) {
   if (c->p_pre) cudaFree(c->p_pre);
   if (c->p_bar) cudaFree(c->p_bar);
   if (c->p_err) cudaFree(c->p_err);
+  if (c->r_ctrs) cudaFree(c->r_ctrs);
+  if (c->r_R) cudaFree(c->r_R);
+  if (c->r_X) cudaFree(c->r_X);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
   return EA_OK;
@@ -1453,7 +1466,7 @@ int ea_sp_sync(ea_sp *c) {
 }
 
 int ea_sp_set_bin_kernel(ea_sp *c, int32_t mode) {
-  if (!c || mode < EA_BIN_AUTO || mode > EA_BIN_PERSISTENT) return spfail(EA_ERR_ARG, "bad bin-kernel mode");
+  if (!c || mode < EA_BIN_AUTO || mode > EA_BIN_RESIDENT) return spfail(EA_ERR_ARG, "bad bin-kernel mode");
   c->bin_mode = mode;
   return EA_OK;
 }
@@ -1483,6 +1496,7 @@ int ea_sp_set_temperatures(ea_sp *c, const double *betas, const uint64_t *cum) {
   SCU(cudaStreamSynchronize(c->st));
   c->d.exptab = c->exptab;
   c->have_temps = true;
+  c->r_state = 0;  // the resident plan stages the exp table: plan again
   return EA_OK;
 }
 
@@ -1552,11 +1566,27 @@ int ea_sp_get_spins(ea_sp *c, uint64_t *S) {
   return EA_OK;
 }
 
+// Whether U2 equals twice the unsatisfied half-edges of the colour-1 sites:
+// two colours, every half-edge's mate at the other end of its bond (on the
+// other colour), and both ends holding the same coupling word.
+static bool sp_pair_energy(const SpGraph &g, int nw, const uint64_t *J) {
+  if (g.ncol != 2) return false;
+  for (int h = 0; h < g.V * 6; ++h) {
+    const int i = h / 6, m = g.mate[h], j = m / 6;
+    if (m < 0 || m >= g.V * 6 || g.nb[h] != j || g.nb[m] != i || g.mate[m] != h || g.colour[i] == g.colour[j])
+      return false;
+    for (int w = 0; w < nw; ++w)
+      if (J[(size_t)w * g.V * 6 + h] != J[(size_t)w * g.V * 6 + m]) return false;
+  }
+  return true;
+}
+
 int ea_sp_set_couplings(ea_sp *c, const uint64_t *J) {
   if (!c || !J) return spfail(EA_ERR_ARG, "null argument");
   SCU(cudaSetDevice(c->device));
   SCU(cudaMemcpyAsync((void *)c->d.J, J, (size_t)c->d.nw * c->d.V * 6 * 8, cudaMemcpyHostToDevice, c->st));
   SCU(cudaStreamSynchronize(c->st));
+  c->pair_energy = sp_pair_energy(c->g, c->d.nw, J);
   return EA_OK;
 }
 
@@ -1720,6 +1750,66 @@ static int sp_run_persist(ea_sp *c, const ea_cadence *cad) {
   return EA_OK;
 }
 
+static bool sp_res_ok(ea_sp *c) {
+  if (c->r_state == 0 || std::memcmp(&c->r_dev, &c->d, sizeof(SpDev))) {
+    c->r_state = sp_res_plan(c->d, c->g.col_sites.data(), c->expoff.empty() ? 0 : c->expoff.back(), c->r_plan) ? 1 : 2;
+    c->r_dev = c->d;
+  }
+  return c->r_state == 1;
+}
+
+// The resident path takes bins without cluster moves of jobs that fit one
+// cluster: explicitly (EA_BIN_RESIDENT) or by default.
+static bool sp_use_resident(ea_sp *c, const ea_cadence *cad) {
+  if (c->bin_mode != EA_BIN_RESIDENT && c->bin_mode != EA_BIN_AUTO) return false;
+  return !cad->cluster && sp_res_launch_sweeps(c->d.V, (size_t)c->d.NR * c->d.NB, cad) > 0 && sp_res_ok(c);
+}
+
+static int sp_run_resident(ea_sp *c, const ea_cadence *cad) {
+  const SpDev &d = c->d;
+  const SpResPlan &pl = c->r_plan;
+  const int spi = cad->mesfr * cad->houfr * cad->ptfr;  // sweeps per iteration
+  const size_t words_sweep = (size_t)3 * d.V * d.NR * d.NB;
+  const size_t nsweep = sp_res_launch_sweeps(d.V, (size_t)d.NR * d.NB, cad), npass = nsweep * d.ncol;
+  const int ipl = (int)(nsweep / spi);  // iterations per launch
+  const size_t npt = (size_t)ipl * cad->mesfr * cad->houfr;
+  if (npass > c->r_cap_pass || nsweep > c->r_cap_sweep || npt > c->r_cap_pt) {
+    SCU(cudaStreamSynchronize(c->st));
+    if (c->r_ctrs) cudaFree(c->r_ctrs);
+    if (c->r_R) cudaFree(c->r_R);
+    if (c->r_X) cudaFree(c->r_X);
+    c->r_ctrs = nullptr;
+    c->r_R = c->r_X = nullptr;
+    c->r_cap_pass = c->r_cap_sweep = c->r_cap_pt = 0;
+    SCU(cudaMalloc((void **)&c->r_ctrs, sizeof(uint4) * npass * d.NR));
+    SCU(cudaMalloc((void **)&c->r_R, 8 * words_sweep * nsweep));
+    SCU(cudaMalloc((void **)&c->r_X, 8 * npt * d.nw * d.NR * (d.NB - 1) * 64));
+    c->r_cap_pass = npass;
+    c->r_cap_sweep = nsweep;
+    c->r_cap_pt = npt;
+  }
+  SpResDev p{};
+  p.d = d;
+  p.R = c->r_R;
+  p.X = c->r_X;
+  p.pair_energy = c->pair_energy ? 1 : 0;
+  p.houfr = cad->houfr;
+  p.mesfr = cad->mesfr;
+  p.ptfr = cad->ptfr;
+  p.ncta = pl.ncta;
+  p.nslm = pl.nslm;
+  p.upc = pl.upc;
+  p.ntab = pl.ntab;
+  std::memcpy(p.kr, pl.kr, sizeof(p.kr));
+  for (int done = 0; done < cad->itmax;) {
+    p.nit = std::min(ipl, cad->itmax - done);
+    p.nsweep = p.nit * spi;
+    SCU(sp_res_chunk(p, pl, p.nsweep * d.ncol, c->r_ctrs, c->st));
+    done += p.nit;
+  }
+  return EA_OK;
+}
+
 int ea_sp_run(ea_sp *c, const ea_cadence *cad, double *avgE) {
   if (!c || !cad || cad->itmax < 1 || cad->houfr < 1 || cad->mesfr < 1 || cad->ptfr < 1)
     return spfail(EA_ERR_ARG, "bad cadence");
@@ -1730,6 +1820,15 @@ int ea_sp_run(ea_sp *c, const ea_cadence *cad, double *avgE) {
   SCU(cudaMemsetAsync(d.avgE, 0, n * 8, c->st));
   int rc, nclust = cad->nclust;
   if (cad->cluster && (rc = sp_cluster_prepare(c, nclust))) return rc;
+  if (c->bin_mode == EA_BIN_RESIDENT && !sp_use_resident(c, cad))
+    return spfail(EA_ERR_ARG, "the resident bin kernel takes bins without cluster moves of jobs whose words fit one "
+                              "thread-block cluster");
+  if (sp_use_resident(c, cad)) {
+    if ((rc = sp_run_resident(c, cad))) return rc;
+    c->last_itmax = cad->itmax;
+    if (avgE) return ea_sp_bin_results(c, avgE);
+    return EA_OK;
+  }
   if (sp_use_persist(c->bin_mode, d)) {
     if ((rc = sp_run_persist(c, cad))) return rc;
     c->last_itmax = cad->itmax;
@@ -2091,6 +2190,12 @@ int ea_sp_job_bytes(const ea_sp_geom *gp, const ea_cadence *cad, const double *b
     const uint64_t nc = (uint64_t)(cad->nclust > 0 ? std::min<int>(cad->nclust, (int)NB) : std::lround(0.5 * NB));
     add(nw * nc * V * 8);
     if (V > (uint64_t)kSpClusterMaxV) add(nw * nc * 8 * sp_cluster_words((int)V) * 4);
+  } else if (cad && sp_res_fits(gp->L, gp->Lz, (int)nw, (int)NR, (int)NB)) {
+    // the resident kernel's counters, random words and tempering uniforms
+    const uint64_t ns = sp_res_launch_sweeps(V, G, cad), spi = (uint64_t)cad->mesfr * cad->houfr * cad->ptfr;
+    add(ns * g.ncol * NR * 16);
+    add(ns * 24 * V * G);
+    if (spi) add(ns / spi * cad->mesfr * cad->houfr * nw * NR * (NB - 1) * 64 * 8);
   }
   *bytes = tot + (2ull << 20);                               // stream, graph, small-allocation pages
   return EA_OK;

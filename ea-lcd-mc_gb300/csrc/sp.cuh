@@ -125,6 +125,42 @@ struct SpPersistDev {
 };
 int sp_persist_grid(const SpBatchDev &b, size_t smem);
 cudaError_t sp_launch_persist(const SpPersistDev &p, int grid, size_t smem, cudaStream_t st);
+
+// Resident bin kernel (sp_resident.cu): bins without cluster moves of a job
+// whose words fit in the shared memory of one thread-block cluster.  CTA c
+// of the cluster owns the z planes [c*ppc, (c+1)*ppc), i.e. the sites
+// [c*nslm, (c+1)*nslm) with nslm = ppc*L*L; the random words of the launch's
+// sweeps are drawn beforehand by k_sp_draw.
+constexpr int kResMaxCta = 16;
+constexpr int kResMaxColours = 8;
+struct SpResDev {
+  SpDev d;
+  const unsigned long long *R;  // [sweep][colour blocks: 3 planes x NR x NB x sites of the colour]
+  const unsigned long long *X;  // [tempering step][word x replica][pair][sample] FNORM * u as bits
+  int nit, nsweep, houfr, mesfr, ptfr;  // iterations and sweeps of this launch, the cadence
+  int pair_energy;               // count the energy in the last colour pass (see ea_sp::pair_energy)
+  int ncta, nslm, upc;           // CTAs, sites per CTA, tempering chains (word, replica) per CTA
+  int ntab;                      // exp table entries staged in SMEM (0: read from global memory)
+  int kr[kResMaxCta + 1][kResMaxColours];  // first index into colour k's site list of CTA c's sites
+};
+struct SpResPlan {
+  int ncta = 0, nslm = 0, upc = 0, ntab = 0, npl = 0;
+  size_t smem = 0;
+  int kr[kResMaxCta + 1][kResMaxColours] = {};
+};
+// Fills `pl` and returns true when the job can run resident (colours, SMEM,
+// a co-resident cluster); col_sites: the host's colour-ordered site list,
+// ntab: entries of the job's exp table.
+bool sp_res_plan(const SpDev &d, const int32_t *col_sites, int ntab, SpResPlan &pl);
+bool sp_res_fits(int L, int Lz, int nw, int NR, int NB);  // the size test of sp_res_plan alone
+// Sweeps of random words one resident launch holds: whole iterations of the
+// cadence, up to 16 MB, at least one iteration; 0 when one iteration's words
+// exceed 256 MB (the resident kernel does not take such bins).
+size_t sp_res_launch_sweeps(size_t V, size_t G, const ea_cadence *cad);
+cudaError_t sp_res_setup();
+// One launch's worth: the counters of npass colour passes, their random
+// words, then the resident kernel over p.nit iterations.
+cudaError_t sp_res_chunk(const SpResDev &p, const SpResPlan &pl, int npass, uint4 *ctrs, cudaStream_t st);
 cudaError_t sp_batch_setup();
 cudaError_t sp_batch_sweep(const SpBatchDev &b, int ncol_max, cudaStream_t st);
 cudaError_t sp_batch_tempering(const SpBatchDev &b, cudaStream_t st);

@@ -46,7 +46,7 @@ class ServerConfig(C.Structure):
 
 
 EA_LAYOUT_MULTISPIN, EA_LAYOUT_SAMPLE_PACKED = 0, 1
-EA_BIN_AUTO, EA_BIN_GRAPH, EA_BIN_PERSISTENT = 0, 1, 2
+EA_BIN_AUTO, EA_BIN_GRAPH, EA_BIN_PERSISTENT, EA_BIN_RESIDENT = 0, 1, 2, 3
 
 
 class Request(C.Structure):
@@ -514,7 +514,7 @@ class SpJob:
         _ck(lib().ea_sp_sync(self.h))
 
     def set_bin_kernel(self, mode):
-        """EA_BIN_AUTO, EA_BIN_GRAPH or EA_BIN_PERSISTENT (ea_sp_set_bin_kernel)."""
+        """EA_BIN_AUTO, EA_BIN_GRAPH, EA_BIN_PERSISTENT or EA_BIN_RESIDENT (ea_sp_set_bin_kernel)."""
         _ck(lib().ea_sp_set_bin_kernel(self.h, int(mode)))
 
     def get_spins(self):

@@ -361,10 +361,18 @@ int ea_sp_bin_results(ea_sp *job, double *avgE);
  * are identical; it removes the per-phase launch gaps that bound jobs too
  * small to fill the GPU.  A barrier wait gives up after 4 s (the kernel
  * returns) and the next ea_sp_sync / ea_sp_bin_results / ea_sp_batch_sync
- * reports EA_ERR_CUDA.  EA_BIN_AUTO (default): the graph, which measured
- * faster on GB300 for a small job alone and for batches of small jobs (a
- * batch's phases in lock-step wait for each phase's slowest job). */
-enum { EA_BIN_AUTO = 0, EA_BIN_GRAPH = 1, EA_BIN_PERSISTENT = 2 };
+ * reports EA_ERR_CUDA.  EA_BIN_RESIDENT (jobs alone, bins without cluster
+ * moves, words that fit in one thread-block cluster of up to 16 CTAs):
+ * per launch of up to 16 MB of random words, the Philox counters of every
+ * colour pass, then all random words on the whole GPU, then one cluster
+ * keeps the spin and coupling words in its distributed shared memory and
+ * runs every sweep, energy count, tempering step and measurement, with the
+ * same results; other bins get EA_ERR_ARG.  EA_BIN_AUTO (default): the
+ * resident kernel where it applies, else the graph (the persistent kernel
+ * measured slower than the graph for a small job alone and for batches of
+ * small jobs: a batch's phases in lock-step wait for each phase's slowest
+ * job).  Batches take AUTO, GRAPH or PERSISTENT. */
+enum { EA_BIN_AUTO = 0, EA_BIN_GRAPH = 1, EA_BIN_PERSISTENT = 2, EA_BIN_RESIDENT = 3 };
 int ea_sp_set_bin_kernel(ea_sp *job, int32_t mode);
 /* Batches of sample-packed jobs (any geometries, replica and temperature
  * counts, up to 4 colours each).  Jobs are grouped in classes (one per job

@@ -120,8 +120,15 @@ def test_job_bytes_cover_the_arrays():
         V = L * L * Lz
         plain = eagb.sp_job_bytes(g, eagb.Cadence(2, 10, 1, 1, 0, 0), betas)
         clus = eagb.sp_job_bytes(g, eagb.Cadence(2, 10, 1, 1, 1, 0), betas)
-        assert plain >= nw * V * NR * 24 * 8 + nw * V * 48
-        assert clus - plain >= nw * 12 * V * 8 + (nw * 12 * 8 * 7 * V if V > 32768 else 0)
+        base = nw * V * NR * 24 * 8 + nw * V * 48
+        assert plain >= base
+        assert clus >= base + nw * 12 * V * 8 + (nw * 12 * 8 * 7 * V if V > 32768 else 0)
+    # a job small enough for the resident kernel is charged its random words
+    # (16 MB per launch here) when its bins have no cluster moves
+    g = eagb.SpGeom(6, 24, 12, 2, 1, eagb.EA_PBC)
+    plain = eagb.sp_job_bytes(g, eagb.Cadence(512, 1, 1, 1, 0, 0), betas[:12])
+    clus = eagb.sp_job_bytes(g, eagb.Cadence(512, 1, 1, 1, 1, 0), betas[:12])
+    assert plain - clus >= 33 * 24 * 864 * 24 - 864 * 6 * 8
     with pytest.raises(eagb.EAError):
         eagb.sp_job_bytes(eagb.SpGeom(1, 4, 24, 2, 1, eagb.EA_PBC))
 
@@ -482,6 +489,69 @@ def test_persistent_bin_kernel_equals_graph(L, Lz, bc, ln, NR, nw, cad):
     assert np.array_equal(b.get_spins(), orc.S)
     assert all(np.array_equal(x, y) for x, y in zip(a.tempering(), b.tempering()))
     assert a.counter() == b.counter() == (orc.it, orc.step)
+    a.close()
+    b.close()
+
+
+# bins without cluster moves: 2 and 3 colours (L=3 and L=7 PBC), 1..3 words,
+# 2..5 replicas, one CTA per z plane up to 16 CTAs of several planes; the
+# first is the L=6, Lz=24 job of the timed configurations with 40 sweeps,
+# two launches of 33 and 7 sweeps (16 MB of random words per launch)
+RESIDENT = [(6, 24, eagb.EA_PBC, "T08_16_N12", 2, 1, (40, 1, 1, 1)),
+            (6, 8, eagb.EA_PBC, "T08_16_N4", 2, 2, (3, 2, 1, 2)),
+            (5, 7, eagb.EA_OBC, "T07_16_N6", 4, 1, (2, 2, 2, 1)),
+            (7, 4, eagb.EA_PBC, "T07_16_N8:7", 5, 3, (2, 3, 1, 1)),
+            (3, 3, eagb.EA_PBC, "T07_16_N8", 2, 1, (3, 1, 1, 3)),
+            (12, 16, eagb.EA_OBC, "T07_16_N12", 4, 2, (2, 5, 1, 1)),
+            (4, 40, eagb.EA_OBC, "T07_16_N6:5", 1, 1, (4, 1, 2, 1))]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("L,Lz,bc,ln,NR,nw,cad", RESIDENT)
+def test_resident_bin_kernel_equals_graph(L, Lz, bc, ln, NR, nw, cad):
+    """The resident bin kernel (counters, random words, then one cluster
+    holding the words in distributed shared memory) and the graph of
+    per-phase launches give the same words, averages, tempering state,
+    counters and generator states, bin after bin; and both equal the
+    oracle."""
+    itmax, houfr, mesfr, ptfr = cad
+    a, b = new_job(L, Lz, bc, ln, NR, nw, jobid=13), new_job(L, Lz, bc, ln, NR, nw, jobid=13)
+    a.set_bin_kernel(eagb.EA_BIN_GRAPH)
+    b.set_bin_kernel(eagb.EA_BIN_RESIDENT)
+    orc = OracleSP(a, 13)
+    for _ in range(2):
+        va = a.run_bin(itmax, houfr, mesfr, ptfr, cluster=False)
+        vb = b.run_bin(itmax, houfr, mesfr, ptfr, cluster=False)
+        want = oracle_bin(orc, itmax, houfr, mesfr, ptfr, False)
+        assert np.array_equal(va, want) and np.array_equal(vb, want)
+    assert np.array_equal(a.get_spins(), b.get_spins())
+    assert np.array_equal(b.get_spins(), orc.S)
+    assert all(np.array_equal(x, y) for x, y in zip(a.tempering(), b.tempering()))
+    assert a.counter() == b.counter() == (orc.it, orc.step)
+    ga, gb = a.get_generators(), b.get_generators()
+    assert bytes(ga) == bytes(gb)
+    assert np.array_equal(a.energy(), b.energy())
+    a.close()
+    b.close()
+
+
+@pytest.mark.gpu
+def test_resident_then_graph_and_moves_continue_alike():
+    """A resident bin followed by a bin with cluster moves (the graph) and
+    another resident bin ends where the graph alone ends; the explicit
+    resident mode refuses a bin with moves."""
+    a = new_job(12, 16, eagb.EA_OBC, "T07_16_N12", 4, 1, jobid=14)
+    b = new_job(12, 16, eagb.EA_OBC, "T07_16_N12", 4, 1, jobid=14)
+    a.set_bin_kernel(eagb.EA_BIN_GRAPH)
+    for cl in (False, True, False):
+        va = a.run_bin(3, 2, 1, 1, cluster=cl)
+        vb = b.run_bin(3, 2, 1, 1, cluster=cl)
+        assert np.array_equal(va, vb)
+    assert np.array_equal(a.get_spins(), b.get_spins())
+    assert a.counter() == b.counter()
+    b.set_bin_kernel(eagb.EA_BIN_RESIDENT)
+    with pytest.raises(RuntimeError):
+        b.run_bin(1, 1, 1, 1, cluster=True)
     a.close()
     b.close()
 
