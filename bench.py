@@ -481,6 +481,7 @@ def run_serve(args, dev, eagb, njobs=240, util=0.8):
 
 # sample-packed layout (64 samples per word): the small-tube and cluster-path
 # configurations, and a wide job of 64 words (4096 samples)
+SP_FORMS = {1: "graph", 2: "persistent", 3: "resident"}
 SP_CASES = [
     # name, L, Lz, bc, lut, NR, nwords, cadence of one step (itmax, houfr, ptfr, cluster), steps
     ("L6_Lz24_PBC_NT12_NR2_64samples_ptfr1", 6, 24, 0, "T08_16_N12", 2, 1, (512, 1, 1, False), 8),
@@ -501,28 +502,40 @@ def run_sp(args, dev, torch, eagb):
         if args.sp_case:
             steps = args.steps
         d = np.load(os.path.join(ROOT, "tests", "golden", "lut_%s.npz" % ln))
-        job = eagb.SpJob(Lx, Lz, d["betas"], d["cum"], nrep=NR, nwords=nw, bc=bc, seeds=MASTERS, device=dev)
-        st = torch.cuda.ExternalStream(job.stream(), device=dev)
         cad = dict(itmax=itmax, houfr=houfr, mesfr=1, ptfr=ptfr, cluster=cl)
-        for _ in range(max(1, args.warmup)):
-            job.run_async(**cad)
-        job.sync()
-        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        t0.record(st)
-        for _ in range(steps):
-            job.run_async(**cad)
-        t1.record(st)
-        job.sync()
-        ms = t0.elapsed_time(t1)
+
+        def timed(mode):
+            job = eagb.SpJob(Lx, Lz, d["betas"], d["cum"], nrep=NR, nwords=nw, bc=bc, seeds=MASTERS, device=dev)
+            job.set_bin_kernel(mode)
+            form = SP_FORMS[job.bin_kernel_for(**cad)]
+            st = torch.cuda.ExternalStream(job.stream(), device=dev)
+            for _ in range(max(1, args.warmup)):
+                job.run_async(**cad)
+            job.sync()
+            t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            t0.record(st)
+            for _ in range(steps):
+                job.run_async(**cad)
+            t1.record(st)
+            job.sync()
+            ncol, kt = job.info()
+            S = job.get_spins()
+            job.close()
+            return t0.elapsed_time(t1), form, ncol, kt, S
+
+        ms, form, ncol, kt, S = timed(eagb.EA_BIN_AUTO)
         V = Lx * Lx * Lz
         sweeps = steps * itmax * houfr * ptfr
         su = sweeps * V * NR * len(d["betas"]) * 64 * nw
-        ncol, kt = job.info()
-        out.append({"workload": name, "value": su / (ms * 1e-3) / 1e12, "unit": "spin-updates/ps",
-                    "sweeps": sweeps, "ms": ms, "us_per_sweep": 1e3 * ms / sweeps, "colours": ncol, "tile": kt,
-                    "samples": 64 * nw, "graph": "one bin iteration replayed as a CUDA graph",
-                    "l2": "job of %.1f MB" % (V * NR * len(d["betas"]) * nw * 8 / 1e6)})
-        job.close()
+        rec = {"workload": name, "value": su / (ms * 1e-3) / 1e12, "unit": "spin-updates/ps",
+               "sweeps": sweeps, "ms": ms, "us_per_sweep": 1e3 * ms / sweeps, "colours": ncol, "tile": kt,
+               "samples": 64 * nw, "bin_kernel": form, "l2": "job of %.1f MB" % (V * NR * len(d["betas"]) * nw * 8 / 1e6)}
+        if form == "resident":
+            # the same bins as a graph of per-phase launches, from the same start
+            gms, _, _, _, gS = timed(eagb.EA_BIN_GRAPH)
+            rec["graph"] = {"us_per_sweep": 1e3 * gms / sweeps, "value": su / (gms * 1e-3) / 1e12,
+                            "bit_exact": bool(np.array_equal(S, gS))}
+        out.append(rec)
     return out
 
 

@@ -1800,6 +1800,8 @@ static int sp_run_resident(ea_sp *c, const ea_cadence *cad) {
   p.nslm = pl.nslm;
   p.upc = pl.upc;
   p.ntab = pl.ntab;
+  p.lpc_count = pl.lpc_count;
+  p.lpc_energy = pl.lpc_energy;
   std::memcpy(p.kr, pl.kr, sizeof(p.kr));
   for (int done = 0; done < cad->itmax;) {
     p.nit = std::min(ipl, cad->itmax - done);
@@ -1807,6 +1809,16 @@ static int sp_run_resident(ea_sp *c, const ea_cadence *cad) {
     SCU(sp_res_chunk(p, pl, p.nsweep * d.ncol, c->r_ctrs, c->st));
     done += p.nit;
   }
+  return EA_OK;
+}
+
+int ea_sp_bin_kernel_for(ea_sp *c, const ea_cadence *cad, int32_t *mode) {
+  if (!c || !cad || !mode || cad->itmax < 1 || cad->houfr < 1 || cad->mesfr < 1 || cad->ptfr < 1)
+    return spfail(EA_ERR_ARG, "bad arguments");
+  SCU(cudaSetDevice(c->device));
+  if (sp_use_resident(c, cad)) *mode = EA_BIN_RESIDENT;
+  else if (c->bin_mode == EA_BIN_RESIDENT) return spfail(EA_ERR_ARG, "the resident bin kernel does not take this bin");
+  else *mode = c->bin_mode == EA_BIN_PERSISTENT ? EA_BIN_PERSISTENT : EA_BIN_GRAPH;
   return EA_OK;
 }
 

@@ -141,10 +141,11 @@ struct SpResDev {
   int pair_energy;               // count the energy in the last colour pass (see ea_sp::pair_energy)
   int ncta, nslm, upc;           // CTAs, sites per CTA, tempering chains (word, replica) per CTA
   int ntab;                      // exp table entries staged in SMEM (0: read from global memory)
+  int lpc_count, lpc_energy;     // lanes per column of the counts in the last pass / the energy phase (8, 16, 32)
   int kr[kResMaxCta + 1][kResMaxColours];  // first index into colour k's site list of CTA c's sites
 };
 struct SpResPlan {
-  int ncta = 0, nslm = 0, upc = 0, ntab = 0, npl = 0;
+  int ncta = 0, nslm = 0, upc = 0, ntab = 0, npl = 0, lpc_count = 32, lpc_energy = 32;
   size_t smem = 0;
   int kr[kResMaxCta + 1][kResMaxColours] = {};
 };

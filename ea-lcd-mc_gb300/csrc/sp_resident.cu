@@ -271,16 +271,18 @@ __device__ __forceinline__ void res_count_add(u64 *P, int npl, const u64 f[6]) {
   }
 }
 
-// A warp's bit-sliced counters summed over its lanes (a butterfly of
-// bit-sliced additions), then samples l and l + 32 of the sum, times `scale`,
-// added by lane l to the counts of the chain (word, replica r) at slot b in
-// the CTA that owns the chain (DSMEM atomics).
+// A group of lpc lanes (8, 16 or 32; one (word, column) per group, lpc | 32)
+// sums its bit-sliced counters (a butterfly of bit-sliced additions inside
+// the group); then lane l of the group holds samples l, l + lpc, ... of the
+// sum and adds them, times `scale`, to the counts of the chain (word,
+// replica r) at slot b in the CTA that owns the chain (DSMEM atomics).
+// Every lane of the warp takes part in the shuffles; `valid` lanes add.
 template <int NPL>
 __device__ __forceinline__ void res_count_flush(const SpResDev &p, const cg::cluster_group &cl, const ResCta &me,
-                                                const ResShared &s, u64 *P, int w, int r, int b, int scale) {
-  const int lane = threadIdx.x & 31, NB = p.d.NB;
-#pragma unroll
-  for (int m = 16; m >= 1; m >>= 1) {
+                                                const ResShared &s, u64 *P, int lpc, bool valid, int w, int r, int b,
+                                                int scale) {
+  const int gl = threadIdx.x & (lpc - 1), NB = p.d.NB;
+  for (int m = lpc >> 1; m >= 1; m >>= 1) {
     u64 cy = 0;
 #pragma unroll
     for (int q = 0; q < NPL; ++q) {
@@ -290,17 +292,27 @@ __device__ __forceinline__ void res_count_flush(const SpResDev &p, const cg::clu
       P[q] = t;
     }
   }
-  int c0 = 0, c1 = 0;
-#pragma unroll
-  for (int q = 0; q < NPL; ++q) {
-    c0 |= (int)((P[q] >> lane) & 1ull) << q;
-    c1 |= (int)((P[q] >> (lane + 32)) & 1ull) << q;
-  }
+  if (!valid) return;
   const int u = w * p.d.NR + r, own = u % p.ncta, lu = u / p.ncta;
-  const size_t o = ((size_t)lu * NB + b) * 64 + lane;
-  int32_t *dst = own == me.rank ? s.U2s : cl.map_shared_rank(s.U2s, own);
-  atomicAdd(dst + o, scale * c0);
-  atomicAdd(dst + o + 32, scale * c1);
+  int32_t *dst = (own == me.rank ? s.U2s : cl.map_shared_rank(s.U2s, own)) + ((size_t)lu * NB + b) * 64;
+  for (int smp = gl; smp < 64; smp += lpc) {
+    int c = 0;
+#pragma unroll
+    for (int q = 0; q < NPL; ++q) c |= (int)((P[q] >> smp) & 1ull) << q;
+    atomicAdd(dst + smp, scale * c);
+  }
+}
+
+// Tempering uniforms of this CTA's chains for step ptj, prefetched into L1
+// ahead of the tempering phase.
+__device__ __forceinline__ void res_prefetch_x(const SpResDev &p, const ResCta &me, int ptj) {
+  const int NP = p.d.NB - 1, nunits = p.d.nw * p.d.NR, per = NP * 4;  // 128-byte lines of a chain's NP x 64 words
+  for (int t = threadIdx.x; t < p.upc * per; t += blockDim.x) {
+    const int lu = t / per, ln = t - lu * per, u = lu * p.ncta + me.rank;
+    if (u >= nunits) continue;
+    const char *a = reinterpret_cast<const char *>(p.X + ((size_t)ptj * nunits + u) * NP * 64) + (size_t)ln * 128;
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(a));
+  }
 }
 
 // The last colour pass of a sweep on a two-colour lattice with the energy
@@ -321,15 +333,18 @@ __device__ __forceinline__ void res_pass_count(const SpResDev &p, const cg::clus
   const u64 *Rk = p.R + (size_t)sweep * 3 * d.V * G + (size_t)3 * off * G + kb;
   const size_t pl = (size_t)nk * G;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-  for (int c = warp; c < d.nw * G; c += nwarp) {
-    const int w = c / G, col = c - w * G, r = col / NB, b = col - r * NB;
-    u64 *Sc = s.S + (size_t)c * nslm;
+  const int lpc = p.lpc_count, cpw = 32 / lpc, gl = lane & (lpc - 1), ncols = d.nw * G;
+  for (int base = warp * cpw; base < ncols; base += nwarp * cpw) {
+    const int c = base + lane / lpc;
+    const bool valid = c < ncols;
+    const int cc = valid ? c : 0, w = cc / G, col = cc - w * G, r = col / NB, b = col - r * NB;
+    u64 *Sc = s.S + (size_t)cc * nslm;
     const u64 *Jw = s.J + (size_t)w * 6 * nslm;
     const u64 *Rc = Rk + (size_t)col * nk;
     u64 P[NPL];
 #pragma unroll
     for (int q = 0; q < NPL; ++q) P[q] = 0;
-    for (int kl = lane; kl < nkc; kl += 32) {
+    for (int kl = gl; valid && kl < nkc; kl += lpc) {
       const int local = s.lst[loff + kl];
       const u64 r0 = __ldg(Rc + kl), r1 = __ldg(Rc + pl + kl), r2 = __ldg(Rc + 2 * pl + kl);
       const u64 sv = Sc[local];
@@ -342,7 +357,7 @@ __device__ __forceinline__ void res_pass_count(const SpResDev &p, const cg::clus
       for (int q = 0; q < 6; ++q) f[q] ^= m;
       res_count_add(P, NPL, f);
     }
-    res_count_flush<NPL>(p, cl, me, s, P, w, r, b, 2);
+    res_count_flush<NPL>(p, cl, me, s, P, lpc, valid, w, r, b, 2);
   }
 }
 
@@ -357,21 +372,24 @@ __device__ __forceinline__ void res_energy(const SpResDev &p, const cg::cluster_
   const SpDev &d = p.d;
   const int NB = d.NB, G = d.NR * NB, nslm = p.nslm;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-  for (int c = warp; c < d.nw * G; c += nwarp) {
-    const int w = c / G, col = c - w * G, r = col / NB, b = col - r * NB;
-    u64 *Sc = s.S + (size_t)c * nslm;
+  const int lpc = p.lpc_energy, cpw = 32 / lpc, gl = lane & (lpc - 1), ncols = d.nw * G;
+  for (int base = warp * cpw; base < ncols; base += nwarp * cpw) {
+    const int c = base + lane / lpc;
+    const bool valid = c < ncols;
+    const int cc = valid ? c : 0, w = cc / G, col = cc - w * G, r = col / NB, b = col - r * NB;
+    u64 *Sc = s.S + (size_t)cc * nslm;
     const u64 *Jw = s.J + (size_t)w * 6 * nslm;
     u64 P[NPL];
 #pragma unroll
     for (int q = 0; q < NPL; ++q) P[q] = 0;
-    for (int i = lane; i < me.nsl; i += 32) {
+    for (int i = gl; valid && i < me.nsl; i += lpc) {
       const u64 sv = Sc[i];
       u64 f[6];
 #pragma unroll
       for (int q = 0; q < 6; ++q) f[q] = sv ^ Jw[(size_t)q * nslm + i] ^ res_word(cl, me, Sc, s.nbl[q * nslm + i]);
       res_count_add(P, NPL, f);
     }
-    res_count_flush<NPL>(p, cl, me, s, P, w, r, b, 1);
+    res_count_flush<NPL>(p, cl, me, s, P, lpc, valid, w, r, b, 1);
   }
 }
 
@@ -553,6 +571,7 @@ __global__ void __launch_bounds__(kResThreads, 1) k_sp_resident(const __grid_con
   for (int it = 0; it < p.nit; ++it)
     for (int im = 0; im < p.mesfr; ++im)
       for (int ih = 0; ih < p.houfr; ++ih) {
+        res_prefetch_x(p, me, ptj);
         for (int sw = 0; sw < p.ptfr; ++sw, ++sweep)
           for (int k = 0; k < ncol; ++k) {
             // the next pass's random words are fetched while this one runs
@@ -606,6 +625,8 @@ __global__ void __launch_bounds__(kResThreads, 1) k_sp_resident(const __grid_con
 // ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
+static int res_lanes(int sites) { return sites <= 32 ? 8 : sites <= 96 ? 16 : 32; }
+
 // Counter planes of the energy phase's warp sums: 6 * nslm < 2^NPL.
 static int res_npl(int nslm) { return 6 * nslm < (1 << 10) ? 10 : kResPlanes; }
 
@@ -685,17 +706,23 @@ bool sp_res_plan(const SpDev &d, const int32_t *col_sites, int ntab, SpResPlan &
       continue;
     }
     if (nclusters < 1) continue;
-    pl.ncta = ncta;
-    pl.nslm = nslm;
-    pl.upc = upc;
-    pl.ntab = nt;
-    pl.npl = npl;
-    pl.smem = smem;
     for (int c = 0; c <= ncta; ++c)
       for (int k = 0; k < d.ncol; ++k) {
         const int32_t *b = col_sites + d.col_off[k], *e2 = col_sites + d.col_off[k + 1];
         pl.kr[c][k] = (int)(std::lower_bound(b, e2, c * nslm) - b);
       }
+    pl.ncta = ncta;
+    pl.nslm = nslm;
+    pl.upc = upc;
+    // lanes per counted column: about 2-4 sites a lane (a butterfly level
+    // costs the same whatever the number of sites behind it)
+    int most = 0;
+    for (int c = 0; c < ncta; ++c) most = std::max(most, pl.kr[c + 1][d.ncol - 1] - pl.kr[c][d.ncol - 1]);
+    pl.lpc_count = res_lanes(most);
+    pl.lpc_energy = res_lanes(nslm);
+    pl.ntab = nt;
+    pl.npl = npl;
+    pl.smem = smem;
     return true;
   }
   return false;

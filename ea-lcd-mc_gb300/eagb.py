@@ -517,6 +517,13 @@ class SpJob:
         """EA_BIN_AUTO, EA_BIN_GRAPH, EA_BIN_PERSISTENT or EA_BIN_RESIDENT (ea_sp_set_bin_kernel)."""
         _ck(lib().ea_sp_set_bin_kernel(self.h, int(mode)))
 
+    def bin_kernel_for(self, itmax, houfr=1, mesfr=1, ptfr=1, cluster=False, nclust=0):
+        """The form ea_sp_run takes for such a bin (ea_sp_bin_kernel_for)."""
+        m = C.c_int32()
+        cad = Cadence(itmax, houfr, mesfr, ptfr, int(cluster), nclust)
+        _ck(lib().ea_sp_bin_kernel_for(self.h, C.byref(cad), C.byref(m)))
+        return m.value
+
     def get_spins(self):
         S = np.zeros((self.g.nwords, self.V, self.g.nrep, self.g.nbetas), np.uint64)
         _ck(lib().ea_sp_get_spins(self.h, P(S)))

@@ -374,6 +374,9 @@ int ea_sp_bin_results(ea_sp *job, double *avgE);
  * job).  Batches take AUTO, GRAPH or PERSISTENT. */
 enum { EA_BIN_AUTO = 0, EA_BIN_GRAPH = 1, EA_BIN_PERSISTENT = 2, EA_BIN_RESIDENT = 3 };
 int ea_sp_set_bin_kernel(ea_sp *job, int32_t mode);
+/* The form (EA_BIN_GRAPH, EA_BIN_PERSISTENT or EA_BIN_RESIDENT) ea_sp_run
+ * takes for a bin of this cadence. */
+int ea_sp_bin_kernel_for(ea_sp *job, const ea_cadence *cad, int32_t *mode);
 /* Batches of sample-packed jobs (any geometries, replica and temperature
  * counts, up to 4 colours each).  Jobs are grouped in classes (one per job
  * for up to 256 jobs, else of equal NB and similar lattice size); each class
