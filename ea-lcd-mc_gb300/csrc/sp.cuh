@@ -128,9 +128,8 @@ cudaError_t sp_launch_persist(const SpPersistDev &p, int grid, size_t smem, cuda
 
 // Resident bin kernel (sp_resident.cu): bins without cluster moves of a job
 // whose words fit in the shared memory of one thread-block cluster.  CTA c
-// of the cluster owns the z planes [c*ppc, (c+1)*ppc), i.e. the sites
-// [c*nslm, (c+1)*nslm) with nslm = ppc*L*L; the random words of the launch's
-// sweeps are drawn beforehand by k_sp_draw.
+// of the cluster owns the sites [c*nslm, (c+1)*nslm); the random words of
+// the launch's sweeps are drawn beforehand by k_sp_draw.
 constexpr int kResMaxCta = 16;
 constexpr int kResMaxColours = 8;
 struct SpResDev {

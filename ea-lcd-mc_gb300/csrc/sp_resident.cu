@@ -14,8 +14,8 @@
 //                   slot) at once on the whole GPU -- the integer-heavy part
 //                   of a sweep, now fully parallel;
 //   k_sp_resident   one cluster of up to 16 CTAs holds the spin and coupling
-//                   words in distributed shared memory (CTA c owns a run of z
-//                   planes) and runs every sweep, energy count, tempering
+//                   words in distributed shared memory (CTA c owns a run of
+//                   sites) and runs every sweep, energy count, tempering
 //                   step, permute and measurement of the chunk, phases
 //                   separated by cluster barriers; neighbour words on other
 //                   CTAs are read through DSMEM.
@@ -165,11 +165,13 @@ struct ResShared {
   int32_t *SG;   // [NB-1] sign of -(beta[i+1] - beta[i])
   uint16_t *lst;
   uint8_t *Ps;
+  u64 *Xs;       // [upc][NB-1][64] tempering uniforms of the step
 };
 
 __host__ __device__ inline size_t res_smem_bytes(int nw, int nslm, int NR, int NB, int upc, int ntab) {
   const size_t G = (size_t)NR * NB, NP = NB - 1, nunits = (size_t)nw * NR, U = (size_t)upc * 64;
-  const size_t b = 8 * ((size_t)nw * nslm * G + (size_t)nw * nslm * 6 + upc * NP + nunits * NP + U * NB + (size_t)ntab) +
+  const size_t b = 8 * ((size_t)nw * nslm * G + (size_t)nw * nslm * 6 + upc * NP + nunits * NP + U * NB + (size_t)ntab +
+                        U * NP) +
                    4 * (2 * U * NB + U * NP + (size_t)nslm * 6 + NB + NP) + 2 * (size_t)nslm + U * NB;
   return (b + 15) & ~(size_t)15;
 }
@@ -182,7 +184,8 @@ __device__ __forceinline__ ResShared res_carve(unsigned char *smem, const SpResD
   s.J = s.S + (size_t)d.nw * p.nslm * G;
   s.Ms = s.J + (size_t)d.nw * p.nslm * 6;
   s.Mall = s.Ms + (size_t)p.upc * NP;
-  s.Av = reinterpret_cast<long long *>(s.Mall + nunits * NP);
+  s.Xs = s.Mall + nunits * NP;
+  s.Av = reinterpret_cast<long long *>(s.Xs + U * NP);
   s.Tab = reinterpret_cast<u64 *>(s.Av + U * d.NB);
   s.U2s = reinterpret_cast<int32_t *>(s.Tab + p.ntab);
   s.Es = s.U2s + U * d.NB;
@@ -202,8 +205,8 @@ __device__ __forceinline__ u64 res_word(const cg::cluster_group &cl, const ResCt
   return own == me.rank ? Sc[nl] : cl.map_shared_rank(Sc, own)[nl];
 }
 
-// One colour pass over the CTA's sites of colour k (sp_pass_body's update),
-// items (word, column, site of the colour) with the site fastest.
+// One colour pass over the CTA's sites of colour k (sp_pass_body's update):
+// a group of lpc lanes per (word, column), lanes over the colour's sites.
 __device__ __forceinline__ void res_pass(const SpResDev &p, const cg::cluster_group &cl, const ResCta &me,
                                          const ResShared &s, int sweep, int k) {
   const SpDev &d = p.d;
@@ -215,39 +218,43 @@ __device__ __forceinline__ void res_pass(const SpResDev &p, const cg::cluster_gr
   for (int c = 0; c < k; ++c) loff += p.kr[me.rank + 1][c] - p.kr[me.rank][c];
   const u64 *Rk = p.R + (size_t)sweep * 3 * d.V * G + (size_t)3 * off * G + kb;
   const size_t pl = (size_t)nk * G;
-  const int items = d.nw * G * nkc;
-  for (int t = threadIdx.x; t < items; t += blockDim.x) {
-    const int c = t / nkc, kl = t - c * nkc, w = c / G, col = c - w * G;
-    const int local = s.lst[loff + kl];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  const int lpc = p.lpc_count, cpw = 32 / lpc, gl = lane & (lpc - 1), ncols = d.nw * G;
+  for (int c = warp * cpw + lane / lpc; c < ncols; c += nwarp * cpw) {
+    const int w = c / G, col = c - w * G;
     u64 *Sc = s.S + (size_t)c * nslm;
-    const size_t e = (size_t)col * nk + kl;
-    const u64 r0 = __ldg(Rk + e), r1 = __ldg(Rk + pl + e), r2 = __ldg(Rk + 2 * pl + e);
-    const u64 sv = Sc[local];
-    const u64 *Jw = s.J + (size_t)w * 6 * nslm + local;
-    u64 f[6];
+    const u64 *Jw = s.J + (size_t)w * 6 * nslm;
+    const u64 *Rc = Rk + (size_t)col * nk;
+    for (int kl = gl; kl < nkc; kl += lpc) {
+      const int local = s.lst[loff + kl];
+      const u64 r0 = __ldg(Rc + kl), r1 = __ldg(Rc + pl + kl), r2 = __ldg(Rc + 2 * pl + kl);
+      const u64 sv = Sc[local];
+      u64 f[6];
 #pragma unroll
-    for (int q = 0; q < 6; ++q) f[q] = sv ^ Jw[(size_t)q * nslm] ^ res_word(cl, me, Sc, s.nbl[q * nslm + local]);
-    Sc[local] = sv ^ flip_mask(f, r0, r1, r2);
+      for (int q = 0; q < 6; ++q) f[q] = sv ^ Jw[(size_t)q * nslm + local] ^ res_word(cl, me, Sc, s.nbl[q * nslm + local]);
+      Sc[local] = sv ^ flip_mask(f, r0, r1, r2);
+    }
   }
 }
 
-// The lines of this CTA's random words of pass (sweep, k), prefetched into L1
-// while the phase before that pass runs.
-__device__ __forceinline__ void res_prefetch(const SpResDev &p, const ResCta &me, int sweep, int k) {
-  const SpDev &d = p.d;
-  if (sweep >= p.nsweep) return;
-  const int G = d.NR * d.NB, off = d.col_off[k], nk = d.col_off[k + 1] - off;
-  const int kb = p.kr[me.rank][k], nkc = p.kr[me.rank + 1][k] - kb;
-  if (nkc <= 0) return;
-  const u64 *base = p.R + (size_t)sweep * 3 * d.V * G + (size_t)3 * off * G + kb;
-  const int per = (nkc * 8 + 127) / 128 + 1;  // lines a (plane, column) run of nkc words can touch
-  for (int t = threadIdx.x; t < 3 * G * per; t += blockDim.x) {
-    const int qc = t / per, ln = t - qc * per;
-    const char *a = reinterpret_cast<const char *>(base + (size_t)qc * nk);
-    const char *e = a + (size_t)nkc * 8 - 1;
-    a += (size_t)ln * 128;
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(a < e ? a : e));
+// Asynchronous 8-byte global-to-SMEM copies (cp.async); a thread waits for
+// all of its copies with cp_async_wait_all (a hardware wait) before the
+// barrier that publishes them.
+__device__ __forceinline__ void cp_async8(void *smem, const void *g) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(g) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Tempering uniforms of this CTA's chains for step ptj into Xs.
+__device__ __forceinline__ void res_stage_x(const SpResDev &p, const ResCta &me, const ResShared &s, int ptj) {
+  const int NP = p.d.NB - 1, nunits = p.d.nw * p.d.NR, per = NP * 64;
+  for (int t = threadIdx.x; t < p.upc * per; t += blockDim.x) {
+    const int lu = t / per, e = t - lu * per, u = lu * p.ncta + me.rank;
+    if (u < nunits) cp_async8(s.Xs + t, p.X + ((size_t)ptj * nunits + u) * per + e);
   }
+  cp_async_commit();
 }
 
 __device__ __forceinline__ void res_count_add(u64 *P, int npl, const u64 f[6]) {
@@ -300,18 +307,6 @@ __device__ __forceinline__ void res_count_flush(const SpResDev &p, const cg::clu
 #pragma unroll
     for (int q = 0; q < NPL; ++q) c |= (int)((P[q] >> smp) & 1ull) << q;
     atomicAdd(dst + smp, scale * c);
-  }
-}
-
-// Tempering uniforms of this CTA's chains for step ptj, prefetched into L1
-// ahead of the tempering phase.
-__device__ __forceinline__ void res_prefetch_x(const SpResDev &p, const ResCta &me, int ptj) {
-  const int NP = p.d.NB - 1, nunits = p.d.nw * p.d.NR, per = NP * 4;  // 128-byte lines of a chain's NP x 64 words
-  for (int t = threadIdx.x; t < p.upc * per; t += blockDim.x) {
-    const int lu = t / per, ln = t - lu * per, u = lu * p.ncta + me.rank;
-    if (u >= nunits) continue;
-    const char *a = reinterpret_cast<const char *>(p.X + ((size_t)ptj * nunits + u) * NP * 64) + (size_t)ln * 128;
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(a));
   }
 }
 
@@ -413,7 +408,7 @@ __device__ __forceinline__ void res_tempering(const SpResDev &p, const ResCta &m
     int32_t *Eo = s.Es + (size_t)lu * NB * 64 + lane;
     uint8_t *Po = s.Ps + (size_t)lu * NB * 64 + lane;
     const int32_t *Uo = s.U2s + (size_t)lu * NB * 64 + lane;
-    const u64 *xo = p.X + ((size_t)ptj * nunits + u) * NP * 64 + lane;
+    const u64 *xo = s.Xs + (size_t)lu * NP * 64 + lane;
     uint32_t *ao = s.As + (size_t)lu * NP * 64 + lane;
     uint32_t *Mh = reinterpret_cast<uint32_t *>(s.Ms + (size_t)lu * NP);
     // the pairs in chunks of 4: every input that does not depend on the
@@ -431,7 +426,7 @@ __device__ __forceinline__ void res_tempering(const SpResDev &p, const ResCta &m
         const int i = min(i0 + j, NP - 1);
         e1[j] = nt - Uo[(i + 1) * 64];
         p1[j] = Po[(i + 1) * 64];
-        x[j] = __ldg(xo + (size_t)i * 64);
+        x[j] = xo[(size_t)i * 64];
         sg[j] = s.SG[i];
         eb[j] = s.EO[i];
         nx[j] = s.EO[i + 1] - eb[j];
@@ -567,18 +562,15 @@ __global__ void __launch_bounds__(kResThreads, 1) k_sp_resident(const __grid_con
   cl.sync();
 
   int sweep = 0, ptj = 0;
-  res_prefetch(p, me, 0, 0);
   for (int it = 0; it < p.nit; ++it)
     for (int im = 0; im < p.mesfr; ++im)
       for (int ih = 0; ih < p.houfr; ++ih) {
-        res_prefetch_x(p, me, ptj);
+        res_stage_x(p, me, s, ptj);
         for (int sw = 0; sw < p.ptfr; ++sw, ++sweep)
           for (int k = 0; k < ncol; ++k) {
-            // the next pass's random words are fetched while this one runs
-            if (k + 1 < ncol) res_prefetch(p, me, sweep, k + 1);
-            else res_prefetch(p, me, sweep + 1, 0);
             if (p.pair_energy && k == ncol - 1 && sw == p.ptfr - 1) res_pass_count<NPL>(p, cl, me, s, sweep, k);
             else res_pass(p, cl, me, s, sweep, k);
+            cp_async_wait_all();  // this step's uniforms (staged before the first pass)
             cl.sync();
           }
         if (!p.pair_energy) {
@@ -661,39 +653,34 @@ static cudaLaunchConfig_t res_config(int ncta, size_t smem, cudaStream_t st, cud
   return cfg;
 }
 
-// Whether the job's share of the widest split (planes split evenly over at
-// most 16 CTAs) fits one CTA's shared memory (the exp table left in global
-// memory).
+// Whether the job's share of the widest split (sites split evenly over 16
+// CTAs) fits one CTA's shared memory (the exp table left in global memory).
 bool sp_res_fits(int L, int Lz, int nw, int NR, int NB) {
   if (NB < 2 || L < 1 || Lz < 1) return false;
-  const int want = std::min(kResMaxCta, Lz), ppc = (Lz + want - 1) / want, ncta = (Lz + ppc - 1) / ppc;
-  const long long nslm = (long long)ppc * L * L;
+  const long long V = (long long)L * L * Lz, nslm = (V + kResMaxCta - 1) / kResMaxCta;
+  const int ncta = (int)((V + nslm - 1) / nslm);
   if (nslm > kResMaxSites) return false;
   const int upc = (nw * NR + ncta - 1) / ncta;
   return res_smem_bytes(nw, (int)nslm, NR, NB, upc, 0) <= 227 * 1024;
 }
 
-// The most CTAs (planes split evenly, at most 16) whose cluster the GPU can
-// hold with the job's shared memory; none when a CTA's share does not fit.
-// The exp table is staged in SMEM when it fits beside the words.
+// The most CTAs (sites split into equal runs, at most 16) whose cluster the
+// GPU can hold with the job's shared memory; none when a CTA's share does
+// not fit.  The exp table is staged in SMEM when it fits beside the words.
 bool sp_res_plan(const SpDev &d, const int32_t *col_sites, int ntab, SpResPlan &pl) {
   if (d.ncol < 1 || d.ncol > kResMaxColours || d.NB < 2) return false;
-  const int L2 = d.L * d.L, nunits = d.nw * d.NR;
+  const int nunits = d.nw * d.NR;
   const size_t lim = 227 * 1024;
   int last = 0;
-  for (int want = std::min(kResMaxCta, d.Lz); want >= 1; --want) {
-    const int ppc = (d.Lz + want - 1) / want, ncta = (d.Lz + ppc - 1) / ppc;
+  for (int want = std::min(kResMaxCta, d.V); want >= 1; --want) {
+    const int nslm = (d.V + want - 1) / want, ncta = (d.V + nslm - 1) / nslm;
     if (ncta == last) continue;
     last = ncta;
-    const int nslm = ppc * L2;
     if (nslm > kResMaxSites) return false;
     const int upc = (nunits + ncta - 1) / ncta;
     int nt = ntab;
     size_t smem = res_smem_bytes(d.nw, nslm, d.NR, d.NB, upc, nt);
-    if (smem > lim) {
-      nt = 0;
-      smem = res_smem_bytes(d.nw, nslm, d.NR, d.NB, upc, 0);
-    }
+    if (smem > lim) smem = res_smem_bytes(d.nw, nslm, d.NR, d.NB, upc, nt = 0);
     if (smem > lim) return false;
     const int npl = res_npl(nslm);
     cudaLaunchAttribute at;
