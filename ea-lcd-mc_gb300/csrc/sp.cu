@@ -171,15 +171,18 @@ constexpr int kSpPlanes = 11;
 // loads per site, so fewer sites a thread is a shorter chain (16 sites a
 // thread measured 16-21 us per count on one-word jobs).
 int sp_energy_chunk(const SpDev &d) {
-  const double words = (double)d.nw * d.V * d.NR * d.NB;
+  const double words = (double)d.nw * d.esites * d.NR * d.NB;
   int c = (int)(words / (152.0 * 2048.0));
   return c < 4 ? 4 : (c > kSpChunkMax ? kSpChunkMax : c);
 }
 
 // col: the thread's index over nw * nchunk * G (blocks of 256 threads).
+// With epair (two colours, both ends of every bond holding its coupling word:
+// checked on the host when the couplings are set) every bond has exactly one
+// colour-1 end, so the count walks the colour-1 sites only and doubles them.
 __device__ __forceinline__ void sp_energy_body(const SpDev &d, long long col) {
-  const int G = d.NR * d.NB, V = d.V, chunk = d.echunk;
-  const int nchunk = (V + chunk - 1) / chunk;
+  const int G = d.NR * d.NB, V = d.V, chunk = d.echunk, ns = d.esites;
+  const int nchunk = (ns + chunk - 1) / chunk;
   if (col >= (long long)d.nw * nchunk * G) return;
   const int rb = (int)(col % G), ch = (int)((col / G) % nchunk), w = (int)(col / ((long long)G * nchunk));
   const u64 *Sw = d.S + (size_t)w * V * G + rb;
@@ -187,13 +190,18 @@ __device__ __forceinline__ void sp_energy_body(const SpDev &d, long long col) {
   u64 P[kSpPlanes];
 #pragma unroll
   for (int p = 0; p < kSpPlanes; ++p) P[p] = 0;
-  const int i0 = ch * chunk, i1 = min(V, i0 + chunk);
-  for (int i = i0; i < i1; ++i) {
-    const u64 sv = Sw[(size_t)i * G];
+  const int i0 = ch * chunk, i1 = min(ns, i0 + chunk);
+  const int32_t *c1 = d.col_sites + d.col_off[1];
+  // two sites an iteration, so that the second site's loads are in flight
+  // while the first is counted (the words are read-only here)
+#pragma unroll 2
+  for (int ii = i0; ii < i1; ++ii) {
+    const int i = d.epair ? __ldg(c1 + ii) : ii;
+    const u64 sv = __ldg(Sw + (size_t)i * G);
     const int *nb = d.nb + (size_t)i * 6;
     u64 f[6];
 #pragma unroll
-    for (int q = 0; q < 6; ++q) f[q] = sv ^ __ldg(Jw + (size_t)i * 6 + q) ^ Sw[(size_t)__ldg(nb + q) * G];
+    for (int q = 0; q < 6; ++q) f[q] = sv ^ __ldg(Jw + (size_t)i * 6 + q) ^ __ldg(Sw + (size_t)__ldg(nb + q) * G);
     // six bits -> a 3-bit count per sample (two full adders and a merge)
     const u64 x1 = f[0] ^ f[1] ^ f[2], y1 = (f[0] & f[1]) | (f[2] & (f[0] ^ f[1]));
     const u64 x2 = f[3] ^ f[4] ^ f[5], y2 = (f[3] & f[4]) | (f[5] & (f[3] ^ f[4]));
@@ -221,7 +229,7 @@ __device__ __forceinline__ void sp_energy_body(const SpDev &d, long long col) {
   for (int lane = 0; lane < 64; ++lane) {
     int cnt = 0;
     for (int p = 0; p < np; ++p) cnt |= (int)((P[p] >> lane) & 1ull) << p;
-    if (cnt) atomicAdd(U + (size_t)lane * G, cnt);
+    if (cnt) atomicAdd(U + (size_t)lane * G, cnt << d.epair);
   }
 }
 
@@ -865,7 +873,7 @@ void sp_batch_blocks(const SpDev &d, bool cluster, uint32_t out[SPB_COUNT]) {
   for (int c = 0; c < kSpBatchMaxColours && c < d.ncol; ++c)
     out[SPB_PASS0 + c] = (uint32_t)((d.col_off[c + 1] - d.col_off[c] + d.kt - 1) / d.kt);
   out[SPB_ZERO] = out[SPB_MEASURE] = (uint32_t)((nw * 64 * G + 255) / 256);
-  out[SPB_ENERGY] = (uint32_t)((nw * ((d.V + d.echunk - 1) / d.echunk) * G + 255) / 256);
+  out[SPB_ENERGY] = (uint32_t)((nw * ((d.esites + d.echunk - 1) / d.echunk) * G + 255) / 256);
   out[SPB_PT] = (uint32_t)(nw * d.NR);
   out[SPB_PERMUTE] = (uint32_t)((nw * d.V * d.NR + kPermRows - 1) / kPermRows);
   if (cluster && d.nclust > 0) {
@@ -1193,7 +1201,7 @@ cudaError_t sp_launch_energy(const SpDev &d, cudaStream_t st) {
   const int G = d.NR * d.NB;
   cudaError_t e = cudaMemsetAsync(d.U2, 0, sizeof(int32_t) * (size_t)d.nw * 64 * G, st);
   if (e != cudaSuccess) return e;
-  const long long n = (long long)d.nw * ((d.V + d.echunk - 1) / d.echunk) * G;
+  const long long n = (long long)d.nw * ((d.esites + d.echunk - 1) / d.echunk) * G;
   k_sp_energy<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d);
   return cudaGetLastError();
 }
@@ -1363,6 +1371,8 @@ int ea_sp_create(const ea_sp_geom *gp, int32_t device, ea_sp **out) {
   int maxc = 0;
   for (int k = 0; k < g.ncol; ++k) maxc = std::max(maxc, g.col_off[k + 1] - g.col_off[k]);
   d.kt = sp_kt(d.NB, d.NR, maxc);
+  d.esites = d.V;
+  d.epair = 0;
   d.echunk = sp_energy_chunk(d);
   for (int k = 0; k <= g.ncol && k < 9; ++k) d.col_off[k] = g.col_off[k];
   if (!d.kt) { delete c; return spfail(EA_ERR_ARG, "NB=%d x NR=%d does not fit in shared memory", d.NB, d.NR); }
@@ -1587,6 +1597,9 @@ int ea_sp_set_couplings(ea_sp *c, const uint64_t *J) {
   SCU(cudaMemcpyAsync((void *)c->d.J, J, (size_t)c->d.nw * c->d.V * 6 * 8, cudaMemcpyHostToDevice, c->st));
   SCU(cudaStreamSynchronize(c->st));
   c->pair_energy = sp_pair_energy(c->g, c->d.nw, J);
+  c->d.epair = c->pair_energy ? 1 : 0;
+  c->d.esites = c->pair_energy ? c->g.col_off[2] - c->g.col_off[1] : c->d.V;
+  c->d.echunk = sp_energy_chunk(c->d);
   return EA_OK;
 }
 
