@@ -90,6 +90,12 @@ struct ea_ctx {
   int hist_cap = 0;
   std::vector<int32_t> expoff;
   double *exptab = nullptr;
+  // staging of whole spin states uploaded from the host (ea_stage_spins_async):
+  // the host copy runs on `cs` into `stage`, beside the job's kernels
+  cudaStream_t cs = nullptr;
+  unsigned long long *stage = nullptr;
+  cudaEvent_t staged = nullptr, stage_free = nullptr;
+  bool stage_pending = false;
   // per-kernel timing (ea_profile)
   bool prof_on = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_ev[EA_K_COUNT];
@@ -444,6 +450,11 @@ int ea_destroy(ea_ctx *c) {
     if (c->drawn[s]) cudaEventDestroy(c->drawn[s]);
     if (c->used[s]) cudaEventDestroy(c->used[s]);
   }
+  if (c->cs) cudaStreamSynchronize(c->cs);
+  if (c->staged) cudaEventDestroy(c->staged);
+  if (c->stage_free) cudaEventDestroy(c->stage_free);
+  if (c->stage) cudaFree(c->stage);
+  if (c->cs) cudaStreamDestroy(c->cs);
   if (c->rs) cudaStreamDestroy(c->rs);
   if (c->st) cudaStreamDestroy(c->st);
   c->st = nullptr;
@@ -467,6 +478,7 @@ int ea_sync(ea_ctx *c) {
   if (check(c)) return EA_ERR_ARG;
   CU(cudaStreamSynchronize(c->st));
   if (c->rs) CU(cudaStreamSynchronize(c->rs));
+  if (c->cs) CU(cudaStreamSynchronize(c->cs));
   return EA_OK;
 }
 
@@ -529,13 +541,41 @@ int ea_set_spins(ea_ctx *c, int32_t s, const uint64_t *even, const uint64_t *odd
   return EA_OK;
 }
 
-int ea_upload_spins_async(ea_ctx *c, const uint64_t *all) {
+int ea_stage_spins_async(ea_ctx *c, const uint64_t *all) {
   if (check(c) || !all) return fail(EA_ERR_ARG, "bad arguments");
   if (set_device(c)) return EA_ERR_CUDA;
   const size_t n = (size_t)c->g.ns * c->g.words_per_sample();
-  CU(cudaMemcpyAsync(c->j.spins, all, n * 8, cudaMemcpyHostToDevice, c->st));
+  if (!c->stage) {
+    CU(cudaStreamCreateWithFlags(&c->cs, cudaStreamNonBlocking));
+    CU(cudaEventCreateWithFlags(&c->staged, cudaEventDisableTiming));
+    CU(cudaEventCreateWithFlags(&c->stage_free, cudaEventDisableTiming));
+    CU(dalloc(c->stage, n));
+    CU(cudaEventRecord(c->stage_free, c->st));
+  }
+  // the buffer is reused once the previous state has been moved out of it
+  CU(cudaStreamWaitEvent(c->cs, c->stage_free, 0));
+  CU(cudaMemcpyAsync(c->stage, all, n * 8, cudaMemcpyHostToDevice, c->cs));
+  CU(cudaEventRecord(c->staged, c->cs));
+  c->stage_pending = true;
+  return EA_OK;
+}
+
+int ea_commit_staged_spins(ea_ctx *c) {
+  if (check(c)) return fail(EA_ERR_ARG, "bad arguments");
+  if (!c->stage_pending) return fail(EA_ERR_STATE, "no staged spin state");
+  if (set_device(c)) return EA_ERR_CUDA;
+  const size_t n = (size_t)c->g.ns * c->g.words_per_sample();
+  CU(cudaStreamWaitEvent(c->st, c->staged, 0));
+  CU(cudaMemcpyAsync(c->j.spins, c->stage, n * 8, cudaMemcpyDeviceToDevice, c->st));
+  CU(cudaEventRecord(c->stage_free, c->st));
+  c->stage_pending = false;
   c->energies_fresh = false;
   return EA_OK;
+}
+
+int ea_upload_spins_async(ea_ctx *c, const uint64_t *all) {
+  const int rc = ea_stage_spins_async(c, all);
+  return rc ? rc : ea_commit_staged_spins(c);
 }
 
 int ea_get_spins(ea_ctx *c, int32_t s, uint64_t *even, uint64_t *odd) {

@@ -141,6 +141,16 @@ int ea_get_spins(ea_ctx *ctx, int32_t sample, uint64_t *even, uint64_t *odd);
  * copy (ea_sync, or a later call that returns data).  No reference
  * counterpart (the reference uploads at start-up and restarts only). */
 int ea_upload_spins_async(ea_ctx *ctx, const uint64_t *all);
+/* The two halves of ea_upload_spins_async, so that the host copy of the next
+ * state can run beside the current kernels: ea_stage_spins_async starts the
+ * host-to-device copy of a whole state (layout as above) into a staging
+ * buffer of the context (allocated at the first call, the size of the spins)
+ * on a copy stream of its own, without touching the job's spins;
+ * ea_commit_staged_spins makes the context's stream wait for that copy and
+ * move the staged state into the spins (a device copy).  The host buffer
+ * must stay unchanged until the commit has been passed by the stream. */
+int ea_stage_spins_async(ea_ctx *ctx, const uint64_t *all);
+int ea_commit_staged_spins(ea_ctx *ctx);
 int ea_set_couplings(ea_ctx *ctx, int32_t sample, const uint64_t *Jw);
 /* pt: [nsamples][NR] PT generators (random_PT, header.h:133). */
 int ea_set_generators(ea_ctx *ctx, const ea_generators *gen, const ea_hq *pt);

@@ -131,4 +131,17 @@ def test_upload_spins_async():
     for s in range(ns):
         ev, od = job.get_spins(s)
         assert np.array_equal(ev, allw[s, 0]) and np.array_equal(od, allw[s, 1])
+    # staged: the job's spins change only at the commit, after the kernels
+    # enqueued before it (here a measurement of the previous state)
+    other = rng.integers(0, 2 ** 63, size=(ns, 2, nw), dtype=np.int64).view(np.uint64)
+    E0 = job.measure_energy()
+    eagb._ck(eagb.lib().ea_stage_spins_async(job.ctx, eagb.P(other)))
+    assert np.array_equal(job.measure_energy(), E0)
+    assert np.array_equal(job.get_spins(0)[0], allw[0, 0])
+    eagb._ck(eagb.lib().ea_commit_staged_spins(job.ctx))
+    job.sync()
+    for s in range(ns):
+        ev, od = job.get_spins(s)
+        assert np.array_equal(ev, other[s, 0]) and np.array_equal(od, other[s, 1])
+    assert eagb.lib().ea_commit_staged_spins(job.ctx) == -4  # EA_ERR_STATE: nothing staged
     job.close()
