@@ -508,6 +508,8 @@ def run_sp(args, dev, torch, eagb):
             job = eagb.SpJob(Lx, Lz, d["betas"], d["cum"], nrep=NR, nwords=nw, bc=bc, seeds=MASTERS, device=dev)
             job.set_bin_kernel(mode)
             form = SP_FORMS[job.bin_kernel_for(**cad)]
+            if form != "resident":
+                tuned[:] = job.autotune()   # tile width, energy sites per thread, labelling block size
             st = torch.cuda.ExternalStream(job.stream(), device=dev)
             for _ in range(max(1, args.warmup)):
                 job.run_async(**cad)
@@ -523,6 +525,7 @@ def run_sp(args, dev, torch, eagb):
             job.close()
             return t0.elapsed_time(t1), form, ncol, kt, S
 
+        tuned = [0, 0, 0]
         ms, form, ncol, kt, S = timed(eagb.EA_BIN_AUTO)
         V = Lx * Lx * Lz
         sweeps = steps * itmax * houfr * ptfr
@@ -530,6 +533,8 @@ def run_sp(args, dev, torch, eagb):
         rec = {"workload": name, "value": su / (ms * 1e-3) / 1e12, "unit": "spin-updates/ps",
                "sweeps": sweeps, "ms": ms, "us_per_sweep": 1e3 * ms / sweeps, "colours": ncol, "tile": kt,
                "samples": 64 * nw, "bin_kernel": form, "l2": "job of %.1f MB" % (V * NR * len(d["betas"]) * nw * 8 / 1e6)}
+        if form != "resident":
+            rec["autotuned"] = {"tile": tuned[0], "energy_sites_per_thread": tuned[1], "labelling_threads": tuned[2]}
         if form == "resident":
             # the same bins as a graph of per-phase launches, from the same start
             gms, _, _, _, gS = timed(eagb.EA_BIN_GRAPH)

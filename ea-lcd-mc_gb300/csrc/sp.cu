@@ -1123,6 +1123,15 @@ cudaError_t sp_launch_persist(const SpPersistDev &p, int grid, size_t smem, cuda
 // One-job kernels: the bodies above, one block per item
 // ---------------------------------------------------------------------------
 __global__ void k_sp_fill(const __grid_constant__ SpDev d) { sp_fill_body(d); }
+// Pseudo-random overlap words (a 64-bit mix of the index) for timing the
+// labelling on clusters of a random overlap; only the autotuner uses it.
+__global__ void k_sp_noise(unsigned long long *Q, long long n) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  unsigned long long x = (unsigned long long)i * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull;
+  x ^= x >> 31; x *= 0xBF58476D1CE4E5B9ull; x ^= x >> 29; x *= 0x94D049BB133111EBull; x ^= x >> 32;
+  Q[i] = x;
+}
 __global__ void __launch_bounds__(512) k_sp_pass(const __grid_constant__ SpDev d, int off, int n) {
   extern __shared__ __align__(16) unsigned char smem[];
   sp_pass_body(d, off, n, blockIdx.x, smem);
@@ -1233,7 +1242,7 @@ cudaError_t sp_launch_houdayer(const SpDev &d, cudaStream_t st) {
   for (int g = 0; g < ng; ++g) {
     const long long n = (long long)d.nw * d.nclust * d.V;
     k_sp_overlap<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d, g);
-    k_sp_cluster<<<(unsigned)(d.nw * d.nclust * 8), sp_cluster_threads(d.V), sp_cluster_smem(d.V), st>>>(d, g);
+    k_sp_cluster<<<(unsigned)(d.nw * d.nclust * 8), d.cthreads, sp_cluster_smem(d.V), st>>>(d, g);
     k_sp_flip<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d, g);
   }
   return cudaGetLastError();
@@ -1371,6 +1380,7 @@ int ea_sp_create(const ea_sp_geom *gp, int32_t device, ea_sp **out) {
   int maxc = 0;
   for (int k = 0; k < g.ncol; ++k) maxc = std::max(maxc, g.col_off[k + 1] - g.col_off[k]);
   d.kt = sp_kt(d.NB, d.NR, maxc);
+  d.cthreads = sp_cluster_threads(d.V);
   d.esites = d.V;
   d.epair = 0;
   d.echunk = sp_energy_chunk(d);
@@ -1623,6 +1633,109 @@ int ea_sp_get_counter(ea_sp *c, int64_t *iter, uint64_t *ptstep) {
   SCU(cudaStreamSynchronize(c->st));
   if (iter) *iter = it;
   if (ptstep) *ptstep = ps;
+  return EA_OK;
+}
+
+// Autotuner: times the launch shapes that leave the results unchanged -- the
+// colour pass's tile width, the energy count's sites per thread and the
+// labelling's block size -- on the job itself and keeps the fastest.  What
+// the timing runs change (spin words, pass counter, Philox counters, the two
+// generators feeding them, the energy counts) is copied aside on the device
+// first and put back after; the labelling runs on pseudo-random overlap words
+// in the job's overlap buffer, which every move rewrites.
+static int sp_sweeps(ea_sp *c, int n);
+static int sp_cluster_prepare(ea_sp *c, int &nclust);
+
+int ea_sp_autotune(ea_sp *c, int32_t *tile, int32_t *echunk, int32_t *cthreads) {
+  if (!c) return spfail(EA_ERR_ARG, "null job");
+  if (!c->have_temps) return spfail(EA_ERR_STATE, "temperatures not set");
+  SCU(cudaSetDevice(c->device));
+  SpDev &d = c->d;
+  const size_t G = (size_t)d.NR * d.NB;
+  struct Part { void *p; size_t n; };
+  const Part parts[] = {{d.S, (size_t)d.nw * d.V * G * 8}, {d.iter, 8}, {d.ctr, sizeof(uint4) * d.NR},
+                        {d.prc, sizeof(ea_hq) * d.NR}, {d.xo, sizeof(ea_xoshiro) * d.NR},
+                        {d.U2, (size_t)d.nw * 64 * G * 4}};
+  size_t total = 0;
+  for (const Part &q : parts) total += (q.n + 255) & ~(size_t)255;
+  char *save = nullptr;
+  SCU(cudaMalloc((void **)&save, total));
+  size_t off = 0;
+  for (const Part &q : parts) {
+    SCU(cudaMemcpyAsync(save + off, q.p, q.n, cudaMemcpyDeviceToDevice, c->st));
+    off += (q.n + 255) & ~(size_t)255;
+  }
+  cudaEvent_t e0, e1;
+  SCU(cudaEventCreate(&e0));
+  SCU(cudaEventCreate(&e1));
+  auto timed = [&](auto &&body) -> float {
+    float best = 1e30f;
+    for (int rep = 0; rep < 3; ++rep) {  // the first run warms up
+      cudaEventRecord(e0, c->st);
+      body();
+      cudaEventRecord(e1, c->st);
+      cudaEventSynchronize(e1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep) best = std::min(best, ms);
+    }
+    return cudaGetLastError() == cudaSuccess ? best : 1e30f;
+  };
+  int maxc = 0;
+  for (int k = 0; k < d.ncol; ++k) maxc = std::max(maxc, d.col_off[k + 1] - d.col_off[k]);
+  // tile width: the heuristic's and its neighbours that fit in SMEM
+  const int kt0 = d.kt;
+  int best_kt = kt0;
+  float best = 1e30f;
+  for (int kt : {kt0 / 2, kt0, kt0 * 2, kt0 * 4}) {
+    if (kt < 1 || kt > 64 || sp_sweep_smem(d.NB, d.NR, kt) > 227 * 1024 - 512) continue;
+    if ((maxc + kt - 1) / kt < 1) continue;
+    d.kt = kt;
+    const float ms = timed([&] { sp_sweeps(c, 2); });
+    if (ms < best) { best = ms; best_kt = kt; }
+  }
+  d.kt = best_kt;
+  // sites per thread of the energy count
+  const int ec0 = d.echunk;
+  int best_ec = ec0;
+  best = 1e30f;
+  for (int ec : {ec0 / 4, ec0 / 2, ec0, ec0 * 2, ec0 * 4}) {
+    if (ec < 1 || ec > 256) continue;
+    d.echunk = ec;
+    const float ms = timed([&] { sp_launch_energy(d, c->st); });
+    if (ms < best) { best = ms; best_ec = ec; }
+  }
+  d.echunk = best_ec;
+  // block size of the labelling (lattices labelled in SMEM)
+  int best_ct = d.cthreads;
+  if (d.V <= kSpClusterMaxV) {
+    int nclust = 0;
+    int rc = sp_cluster_prepare(c, nclust);
+    if (rc) { cudaFree(save); return rc; }
+    const long long nq = (long long)d.nw * d.nclust * d.V;
+    best = 1e30f;
+    for (int ct : {256, 512, 1024}) {
+      const float ms = timed([&] {
+        k_sp_noise<<<(unsigned)((nq + 255) / 256), 256, 0, c->st>>>(d.Q, nq);
+        k_sp_cluster<<<(unsigned)(d.nw * d.nclust * 8), ct, sp_cluster_smem(d.V), c->st>>>(d, 0);
+      });
+      if (ms < best) { best = ms; best_ct = ct; }
+    }
+  }
+  d.cthreads = best_ct;
+  off = 0;
+  for (const Part &q : parts) {
+    cudaMemcpyAsync(q.p, save + off, q.n, cudaMemcpyDeviceToDevice, c->st);
+    off += (q.n + 255) & ~(size_t)255;
+  }
+  const cudaError_t e = cudaStreamSynchronize(c->st);
+  cudaFree(save);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  SCU(e);
+  if (tile) *tile = d.kt;
+  if (echunk) *echunk = d.echunk;
+  if (cthreads) *cthreads = d.cthreads;
   return EA_OK;
 }
 

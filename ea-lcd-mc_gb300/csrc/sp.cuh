@@ -40,6 +40,7 @@ struct SpDev {
   int L, Lz, V, bc, NB, NR, nw, ncol, kt;
   int echunk;                        // sites per thread of the energy count
   int esites, epair;                 // sites the count walks: all V, or (epair = 1) the colour-1 sites, counted twice
+  int cthreads;                      // block size of the one-job cluster labelling
   int col_off[9];                    // colour c owns col_sites[col_off[c] .. col_off[c+1])
   const int32_t *nb;                 // [V][6]
   const int32_t *col_sites;          // [V]

@@ -517,6 +517,12 @@ class SpJob:
         """EA_BIN_AUTO, EA_BIN_GRAPH, EA_BIN_PERSISTENT or EA_BIN_RESIDENT (ea_sp_set_bin_kernel)."""
         _ck(lib().ea_sp_set_bin_kernel(self.h, int(mode)))
 
+    def autotune(self):
+        """ea_sp_autotune: (tile width, energy sites per thread, labelling block size) chosen."""
+        kt, ec, ct = C.c_int32(), C.c_int32(), C.c_int32()
+        _ck(lib().ea_sp_autotune(self.h, C.byref(kt), C.byref(ec), C.byref(ct)))
+        return kt.value, ec.value, ct.value
+
     def bin_kernel_for(self, itmax, houfr=1, mesfr=1, ptfr=1, cluster=False, nclust=0):
         """The form ea_sp_run takes for such a bin (ea_sp_bin_kernel_for)."""
         m = C.c_int32()

@@ -387,6 +387,13 @@ int ea_sp_set_bin_kernel(ea_sp *job, int32_t mode);
 /* The form (EA_BIN_GRAPH, EA_BIN_PERSISTENT or EA_BIN_RESIDENT) ea_sp_run
  * takes for a bin of this cadence. */
 int ea_sp_bin_kernel_for(ea_sp *job, const ea_cadence *cad, int32_t *mode);
+/* Autotuner (no reference counterpart): times, on the job itself, the launch
+ * shapes that leave every result unchanged -- the colour pass's tile width,
+ * the energy count's sites per thread and the cluster labelling's block size
+ * -- and keeps the fastest of each; the job's state is saved on the device
+ * and put back, so its results are those of the untuned job.  Allocates the
+ * overlap buffer of the cluster moves if it is missing.  Outputs may be NULL. */
+int ea_sp_autotune(ea_sp *job, int32_t *tile, int32_t *echunk, int32_t *cthreads);
 /* Batches of sample-packed jobs (any geometries, replica and temperature
  * counts, up to 4 colours each).  Jobs are grouped in classes (one per job
  * for up to 256 jobs, else of equal NB and similar lattice size); each class

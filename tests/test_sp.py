@@ -536,6 +536,34 @@ def test_resident_bin_kernel_equals_graph(L, Lz, bc, ln, NR, nw, cad):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("L,Lz,bc,ln,NR,nw", [(12, 48, eagb.EA_OBC, "T07_16_N24", 4, 2),
+                                              (7, 4, eagb.EA_PBC, "T07_16_N8:7", 5, 3)])
+def test_autotuned_job_equals_untuned(L, Lz, bc, ln, NR, nw):
+    """The autotuner leaves the job's state as it was, and the job with the
+    tuned tile width, energy chunking and labelling block size gives the same
+    words, averages, tempering state and counters as the untuned one, with and
+    without cluster moves (graph path) -- and both equal the oracle."""
+    a, b = new_job(L, Lz, bc, ln, NR, nw, jobid=15), new_job(L, Lz, bc, ln, NR, nw, jobid=15)
+    a.set_bin_kernel(eagb.EA_BIN_GRAPH)
+    b.set_bin_kernel(eagb.EA_BIN_GRAPH)
+    S0, c0 = b.get_spins(), b.counter()
+    kt, ec, ct = b.autotune()
+    assert kt >= 1 and ec >= 1 and ct in (256, 512, 1024)
+    assert np.array_equal(b.get_spins(), S0) and b.counter() == c0
+    orc = OracleSP(a, 15)
+    for cl in (True, False):
+        va = a.run_bin(2, 2, 1, 1, cluster=cl)
+        vb = b.run_bin(2, 2, 1, 1, cluster=cl)
+        assert np.array_equal(va, vb)
+        assert np.array_equal(va, oracle_bin(orc, 2, 2, 1, 1, cl))
+    assert np.array_equal(a.get_spins(), b.get_spins())
+    assert all(np.array_equal(x, y) for x, y in zip(a.tempering(), b.tempering()))
+    assert a.counter() == b.counter()
+    a.close()
+    b.close()
+
+
+@pytest.mark.gpu
 def test_resident_then_graph_and_moves_continue_alike():
     """A resident bin followed by a bin with cluster moves (the graph) and
     another resident bin ends where the graph alone ends; the explicit
