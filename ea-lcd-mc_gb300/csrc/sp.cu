@@ -1888,7 +1888,7 @@ static bool sp_res_ok(ea_sp *c) {
 // cluster: explicitly (EA_BIN_RESIDENT) or by default.
 static bool sp_use_resident(ea_sp *c, const ea_cadence *cad) {
   if (c->bin_mode != EA_BIN_RESIDENT && c->bin_mode != EA_BIN_AUTO) return false;
-  return !cad->cluster && sp_res_launch_sweeps(c->d.V, (size_t)c->d.NR * c->d.NB, cad) > 0 && sp_res_ok(c);
+  return sp_res_launch_sweeps(c->d.V, (size_t)c->d.NR * c->d.NB, cad) > 0 && sp_res_ok(c);
 }
 
 static int sp_run_resident(ea_sp *c, const ea_cadence *cad) {
@@ -1897,8 +1897,8 @@ static int sp_run_resident(ea_sp *c, const ea_cadence *cad) {
   const int spi = cad->mesfr * cad->houfr * cad->ptfr;  // sweeps per iteration
   const size_t words_sweep = (size_t)3 * d.V * d.NR * d.NB;
   const size_t nsweep = sp_res_launch_sweeps(d.V, (size_t)d.NR * d.NB, cad), npass = nsweep * d.ncol;
-  const int ipl = (int)(nsweep / spi);  // iterations per launch
-  const size_t npt = (size_t)ipl * cad->mesfr * cad->houfr;
+  const int ipl = cad->cluster ? 1 : (int)(nsweep / spi);  // iterations per launch
+  const size_t npt = nsweep / cad->ptfr;                    // tempering steps per launch
   if (npass > c->r_cap_pass || nsweep > c->r_cap_sweep || npt > c->r_cap_pt) {
     SCU(cudaStreamSynchronize(c->st));
     if (c->r_ctrs) cudaFree(c->r_ctrs);
@@ -1929,6 +1929,26 @@ static int sp_run_resident(ea_sp *c, const ea_cadence *cad) {
   p.lpc_count = pl.lpc_count;
   p.lpc_energy = pl.lpc_energy;
   std::memcpy(p.kr, pl.kr, sizeof(p.kr));
+  if (cad->cluster) {
+    // per houfr block: one resident launch (sweeps and tempering steps, no
+    // measurement), then the move's kernels on the words it wrote back; the
+    // energies counted again and measured after each iteration, as the
+    // graph path does
+    p.nit = 1;
+    p.mesfr = 1;
+    p.nsweep = (int)nsweep;
+    p.measure = 0;
+    for (int it = 0; it < cad->itmax; ++it) {
+      for (int im = 0; im < cad->mesfr; ++im) {
+        SCU(sp_res_chunk(p, pl, p.nsweep * d.ncol, c->r_ctrs, c->st));
+        SCU(sp_launch_houdayer(c->d, c->st));
+      }
+      SCU(sp_launch_energy(c->d, c->st));
+      SCU(sp_launch_measure_u2(c->d, false, c->st));
+    }
+    return EA_OK;
+  }
+  p.measure = 1;
   for (int done = 0; done < cad->itmax;) {
     p.nit = std::min(ipl, cad->itmax - done);
     p.nsweep = p.nit * spi;
@@ -1959,8 +1979,8 @@ int ea_sp_run(ea_sp *c, const ea_cadence *cad, double *avgE) {
   int rc, nclust = cad->nclust;
   if (cad->cluster && (rc = sp_cluster_prepare(c, nclust))) return rc;
   if (c->bin_mode == EA_BIN_RESIDENT && !sp_use_resident(c, cad))
-    return spfail(EA_ERR_ARG, "the resident bin kernel takes bins without cluster moves of jobs whose words fit one "
-                              "thread-block cluster");
+    return spfail(EA_ERR_ARG, "the resident bin kernel takes jobs whose words fit one thread-block cluster, bins "
+                              "without cluster moves or with at least %d sweeps between moves", kResMinBlock);
   if (sp_use_resident(c, cad)) {
     if ((rc = sp_run_resident(c, cad))) return rc;
     c->last_itmax = cad->itmax;
@@ -2328,12 +2348,13 @@ int ea_sp_job_bytes(const ea_sp_geom *gp, const ea_cadence *cad, const double *b
     const uint64_t nc = (uint64_t)(cad->nclust > 0 ? std::min<int>(cad->nclust, (int)NB) : std::lround(0.5 * NB));
     add(nw * nc * V * 8);
     if (V > (uint64_t)kSpClusterMaxV) add(nw * nc * 8 * sp_cluster_words((int)V) * 4);
-  } else if (cad && sp_res_fits(gp->L, gp->Lz, (int)nw, (int)NR, (int)NB)) {
+  }
+  if (cad && sp_res_fits(gp->L, gp->Lz, (int)nw, (int)NR, (int)NB)) {
     // the resident kernel's counters, random words and tempering uniforms
-    const uint64_t ns = sp_res_launch_sweeps(V, G, cad), spi = (uint64_t)cad->mesfr * cad->houfr * cad->ptfr;
+    const uint64_t ns = sp_res_launch_sweeps(V, G, cad);
     add(ns * g.ncol * NR * 16);
     add(ns * 24 * V * G);
-    if (spi) add(ns / spi * cad->mesfr * cad->houfr * nw * NR * (NB - 1) * 64 * 8);
+    if (cad->ptfr > 0) add(ns / cad->ptfr * nw * NR * (NB - 1) * 64 * 8);
   }
   *bytes = tot + (2ull << 20);                               // stream, graph, small-allocation pages
   return EA_OK;

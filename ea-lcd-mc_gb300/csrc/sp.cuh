@@ -133,6 +133,7 @@ cudaError_t sp_launch_persist(const SpPersistDev &p, int grid, size_t smem, cuda
 // of the cluster owns the sites [c*nslm, (c+1)*nslm); the random words of
 // the launch's sweeps are drawn beforehand by k_sp_draw.
 constexpr int kResMaxCta = 16;
+constexpr int kResMinBlock = 4;  // fewest sweeps between cluster moves for a resident launch to pay
 constexpr int kResMaxColours = 8;
 struct SpResDev {
   SpDev d;
@@ -140,6 +141,7 @@ struct SpResDev {
   const unsigned long long *X;  // [tempering step][word x replica][pair][sample] FNORM * u as bits
   int nit, nsweep, houfr, mesfr, ptfr;  // iterations and sweeps of this launch, the cadence
   int pair_energy;               // count the energy in the last colour pass (see ea_sp::pair_energy)
+  int measure;                   // add the energies to the bin's sums after each iteration (no cluster moves)
   int ncta, nslm, upc;           // CTAs, sites per CTA, tempering chains (word, replica) per CTA
   int ntab;                      // exp table entries staged in SMEM (0: read from global memory)
   int lpc_count, lpc_energy;     // lanes per column of the counts in the last pass / the energy phase (8, 16, 32)
@@ -156,8 +158,10 @@ struct SpResPlan {
 bool sp_res_plan(const SpDev &d, const int32_t *col_sites, int ntab, SpResPlan &pl);
 bool sp_res_fits(int L, int Lz, int nw, int NR, int NB);  // the size test of sp_res_plan alone
 // Sweeps of random words one resident launch holds: whole iterations of the
-// cadence, up to 16 MB, at least one iteration; 0 when one iteration's words
-// exceed 256 MB (the resident kernel does not take such bins).
+// cadence, up to 16 MB, at least one iteration; with cluster moves one block
+// of houfr x ptfr sweeps (at least kResMinBlock) between two moves; 0 when
+// that exceeds 256 MB or the block is shorter (the resident kernel does not
+// take such bins).
 size_t sp_res_launch_sweeps(size_t V, size_t G, const ea_cadence *cad);
 cudaError_t sp_res_setup();
 // One launch's worth: the counters of npass colour passes, their random

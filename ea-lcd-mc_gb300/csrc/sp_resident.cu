@@ -577,8 +577,8 @@ __global__ void __launch_bounds__(kResThreads, 1) k_sp_resident(const __grid_con
           res_energy<NPL>(p, cl, me, s);
           cl.sync();
         }
-        const bool meas = im == p.mesfr - 1 && ih == p.houfr - 1;
-        res_tempering(p, me, s, ptj, meas, meas && it == p.nit - 1);
+        const bool lastpt = im == p.mesfr - 1 && ih == p.houfr - 1;
+        res_tempering(p, me, s, ptj, p.measure && lastpt, lastpt && it == p.nit - 1);
         cl.sync();
         res_permute(p, cl, me, s);
         cl.sync();
@@ -717,6 +717,11 @@ bool sp_res_plan(const SpDev &d, const int32_t *col_sites, int ntab, SpResPlan &
 
 size_t sp_res_launch_sweeps(size_t V, size_t G, const ea_cadence *cad) {
   const size_t spi = (size_t)cad->mesfr * cad->houfr * cad->ptfr, bytes_sweep = 24 * V * G;
+  if (cad->cluster) {
+    // one launch per block of houfr x ptfr sweeps between two cluster moves
+    const size_t blk = (size_t)cad->houfr * cad->ptfr;
+    return blk >= (size_t)kResMinBlock && blk * bytes_sweep <= ((size_t)256 << 20) ? blk : 0;
+  }
   if (spi * bytes_sweep > ((size_t)256 << 20)) return 0;
   const size_t its = std::max<size_t>(1, ((size_t)16 << 20) / (bytes_sweep * spi));
   return std::min(its, (size_t)std::max(cad->itmax, 1)) * spi;

@@ -371,13 +371,15 @@ int ea_sp_bin_results(ea_sp *job, double *avgE);
  * are identical; it removes the per-phase launch gaps that bound jobs too
  * small to fill the GPU.  A barrier wait gives up after 4 s (the kernel
  * returns) and the next ea_sp_sync / ea_sp_bin_results / ea_sp_batch_sync
- * reports EA_ERR_CUDA.  EA_BIN_RESIDENT (jobs alone, bins without cluster
- * moves, words that fit in one thread-block cluster of up to 16 CTAs):
- * per launch of up to 16 MB of random words, the Philox counters of every
- * colour pass, then all random words on the whole GPU, then one cluster
- * keeps the spin and coupling words in its distributed shared memory and
- * runs every sweep, energy count, tempering step and measurement, with the
- * same results; other bins get EA_ERR_ARG.  EA_BIN_AUTO (default): the
+ * reports EA_ERR_CUDA.  EA_BIN_RESIDENT (jobs alone whose words fit in one
+ * thread-block cluster of up to 16 CTAs): per launch of up to 16 MB of
+ * random words, the Philox counters of every colour pass, then all random
+ * words on the whole GPU, then one cluster keeps the spin and coupling
+ * words in its distributed shared memory and runs every sweep, energy
+ * count, tempering step and measurement, with the same results; with
+ * cluster moves every block of houfr x ptfr >= 4 sweeps is one such launch
+ * and the moves run as per-phase launches between them; other bins get
+ * EA_ERR_ARG.  EA_BIN_AUTO (default): the
  * resident kernel where it applies, else the graph (the persistent kernel
  * measured slower than the graph for a small job alone and for batches of
  * small jobs: a batch's phases in lock-step wait for each phase's slowest

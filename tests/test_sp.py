@@ -497,32 +497,40 @@ def test_persistent_bin_kernel_equals_graph(L, Lz, bc, ln, NR, nw, cad):
 # 2..5 replicas, one CTA per z plane up to 16 CTAs of several planes; the
 # first is the L=6, Lz=24 job of the timed configurations with 40 sweeps,
 # two launches of 33 and 7 sweeps (16 MB of random words per launch)
-RESIDENT = [(6, 24, eagb.EA_PBC, "T08_16_N12", 2, 1, (40, 1, 1, 1)),
-            (6, 8, eagb.EA_PBC, "T08_16_N4", 2, 2, (3, 2, 1, 2)),
-            (5, 7, eagb.EA_OBC, "T07_16_N6", 4, 1, (2, 2, 2, 1)),
-            (7, 4, eagb.EA_PBC, "T07_16_N8:7", 5, 3, (2, 3, 1, 1)),
-            (3, 3, eagb.EA_PBC, "T07_16_N8", 2, 1, (3, 1, 1, 3)),
-            (12, 16, eagb.EA_OBC, "T07_16_N12", 4, 2, (2, 5, 1, 1)),
-            (4, 40, eagb.EA_OBC, "T07_16_N6:5", 1, 1, (4, 1, 2, 1))]
+RESIDENT = [(6, 24, eagb.EA_PBC, "T08_16_N12", 2, 1, (40, 1, 1, 1, False)),
+            (6, 8, eagb.EA_PBC, "T08_16_N4", 2, 2, (3, 2, 1, 2, False)),
+            (5, 7, eagb.EA_OBC, "T07_16_N6", 4, 1, (2, 2, 2, 1, False)),
+            (7, 4, eagb.EA_PBC, "T07_16_N8:7", 5, 3, (2, 3, 1, 1, False)),
+            (3, 3, eagb.EA_PBC, "T07_16_N8", 2, 1, (3, 1, 1, 3, False)),
+            (12, 16, eagb.EA_OBC, "T07_16_N12", 4, 2, (2, 5, 1, 1, False)),
+            (4, 40, eagb.EA_OBC, "T07_16_N6:5", 1, 1, (4, 1, 2, 1, False)),
+            # cluster moves between resident launches of houfr x ptfr >= 4 sweeps
+            (6, 8, eagb.EA_PBC, "T08_16_N4", 4, 1, (3, 5, 1, 1, True)),
+            (5, 7, eagb.EA_OBC, "T07_16_N6", 4, 1, (2, 4, 2, 1, True)),
+            (7, 4, eagb.EA_PBC, "T07_16_N8:7", 5, 3, (2, 2, 1, 2, True)),
+            (12, 16, eagb.EA_OBC, "T07_16_N12", 4, 2, (2, 10, 1, 1, True)),
+            (6, 12, eagb.EA_OBC, "T07_16_N6", 2, 1, (3, 4, 1, 1, True))]
 
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("L,Lz,bc,ln,NR,nw,cad", RESIDENT)
 def test_resident_bin_kernel_equals_graph(L, Lz, bc, ln, NR, nw, cad):
     """The resident bin kernel (counters, random words, then one cluster
-    holding the words in distributed shared memory) and the graph of
+    holding the words in distributed shared memory; with cluster moves, one
+    launch per block of sweeps and the moves between them) and the graph of
     per-phase launches give the same words, averages, tempering state,
     counters and generator states, bin after bin; and both equal the
     oracle."""
-    itmax, houfr, mesfr, ptfr = cad
+    itmax, houfr, mesfr, ptfr, cl = cad
     a, b = new_job(L, Lz, bc, ln, NR, nw, jobid=13), new_job(L, Lz, bc, ln, NR, nw, jobid=13)
     a.set_bin_kernel(eagb.EA_BIN_GRAPH)
     b.set_bin_kernel(eagb.EA_BIN_RESIDENT)
     orc = OracleSP(a, 13)
+    assert b.bin_kernel_for(itmax, houfr, mesfr, ptfr, cluster=cl) == eagb.EA_BIN_RESIDENT
     for _ in range(2):
-        va = a.run_bin(itmax, houfr, mesfr, ptfr, cluster=False)
-        vb = b.run_bin(itmax, houfr, mesfr, ptfr, cluster=False)
-        want = oracle_bin(orc, itmax, houfr, mesfr, ptfr, False)
+        va = a.run_bin(itmax, houfr, mesfr, ptfr, cluster=cl)
+        vb = b.run_bin(itmax, houfr, mesfr, ptfr, cluster=cl)
+        want = oracle_bin(orc, itmax, houfr, mesfr, ptfr, cl)
         assert np.array_equal(va, want) and np.array_equal(vb, want)
     assert np.array_equal(a.get_spins(), b.get_spins())
     assert np.array_equal(b.get_spins(), orc.S)
