@@ -20,7 +20,7 @@ CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-I" + os.path.join(ROOT, "include"), "-I" + CSRC, "-Xcompiler", "-fPIC"]
-SOURCES = ["kernels.cu", "batch.cu", "api.cu", "host.cpp", "noalloc.cu", "serve.cpp", "sp.cu", "sp_resident.cu", "sp_host.cpp", "probe.cu"]
+SOURCES = ["kernels.cu", "batch.cu", "api.cu", "host.cpp", "noalloc.cu", "serve.cpp", "sp.cu", "sp_resident.cu", "sp_analysis.cu", "sp_host.cpp", "probe.cu"]
 
 
 def _compile(src):

@@ -1452,6 +1452,16 @@ int ea_sp_destroy(ea_sp *c) {
   return EA_OK;
 }
 
+// The job's device view and stream, for the analysis entry points of
+// sp_analysis.cu (current device set to the job's).
+int ea_sp_device_view(ea_sp *c, SpDev *d, cudaStream_t *st) {
+  if (!c || !d || !st) return spfail(EA_ERR_ARG, "null argument");
+  SCU(cudaSetDevice(c->device));
+  *d = c->d;
+  *st = c->st;
+  return EA_OK;
+}
+
 int ea_sp_info(const ea_sp *c, int32_t *ncol, int32_t *tile) {
   if (!c) return spfail(EA_ERR_ARG, "null job");
   if (ncol) *ncol = c->d.ncol;

@@ -517,6 +517,20 @@ class SpJob:
         """EA_BIN_AUTO, EA_BIN_GRAPH, EA_BIN_PERSISTENT or EA_BIN_RESIDENT (ea_sp_set_bin_kernel)."""
         _ck(lib().ea_sp_set_bin_kernel(self.h, int(mode)))
 
+    def plane_overlaps(self, nrep):
+        """ea_sp_plane_overlaps: differing spins per (word, sample, pair, slot, plane)."""
+        g = self.g
+        out = np.zeros((g.nwords, 64, nrep // 2, g.nbetas, g.Lz), np.int32)
+        _ck(lib().ea_sp_plane_overlaps(self.h, int(nrep), P(out)))
+        return out
+
+    def plane_correlations(self, nrep, dmax):
+        """ea_sp_plane_correlations: [samples][slot][d][3][3] correlation matrices."""
+        g = self.g
+        out = np.zeros((g.nwords * 64, g.nbetas, dmax + 1, 3, 3))
+        _ck(lib().ea_sp_plane_correlations(self.h, int(nrep), int(dmax), P(out)))
+        return out
+
     def autotune(self):
         """ea_sp_autotune: (tile width, energy sites per thread, labelling block size) chosen."""
         kt, ec, ct = C.c_int32(), C.c_int32(), C.c_int32()

@@ -396,6 +396,20 @@ int ea_sp_bin_kernel_for(ea_sp *job, const ea_cadence *cad, int32_t *mode);
  * and put back, so its results are those of the untuned job.  Allocates the
  * overlap buffer of the cluster moves if it is missing.  Outputs may be NULL. */
 int ea_sp_autotune(ea_sp *job, int32_t *tile, int32_t *echunk, int32_t *cthreads);
+/* Configuration analysis of the job's current spins (no reference code; the
+ * reference's DATA/README.md describes correlation functions of the overlap
+ * built from f, g in {x, x^3, sign x} with r = 2, 4, 6, 8 replicas).  The
+ * replica pairs are (0,1), (2,3), ... among the first nrep replicas (even,
+ * <= NR); the plane overlap of a pair at a temperature slot and plane z is
+ * q_z = 1 - 2 diff_z / L^2, diff_z = spins that differ on the plane (planes
+ * of at most 4095 sites).
+ * ea_sp_plane_overlaps: diff [nwords][64][nrep/2][NB][Lz].
+ * ea_sp_plane_correlations: C [nwords*64][NB][dmax+1][3][3], entry [f][g] =
+ * mean over the pairs and planes z of f(q_z) g(q_{z+d}) for f, g in
+ * (x, x^3, sign x); z + d taken modulo Lz under PBC, only z + d < Lz with
+ * open boundaries; dmax < Lz. */
+int ea_sp_plane_overlaps(ea_sp *job, int32_t nrep, int32_t *diff);
+int ea_sp_plane_correlations(ea_sp *job, int32_t nrep, int32_t dmax, double *C);
 /* Batches of sample-packed jobs (any geometries, replica and temperature
  * counts, up to 4 colours each).  Jobs are grouped in classes (one per job
  * for up to 256 jobs, else of equal NB and similar lattice size); each class
