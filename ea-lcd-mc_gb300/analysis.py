@@ -2,9 +2,11 @@
 functions and the reference's data-file layout.
 
 The per-sample correlation matrices come from ea_sp_plane_correlations
-(`SpJob.plane_correlations(nrep, dmax)`): C[sample][slot][d][f][g], f, g in
-(x, x^3, sign x) of the plane overlap q.  From them, per temperature slot and
-distance d (the abscissa):
+(`SpJob.plane_correlations(nrep, dmax)`, on the GPU) for sample-packed jobs,
+or from `multispin_plane_diff` + `plane_correlations` (on the host) for
+configurations in the reference's multispin layout: C[sample][slot][d][f][g],
+f, g in (x, x^3, sign x) of the plane overlap q.  From them, per temperature
+slot and distance d (the abscissa):
 
     C_fg(d)        the sample mean; normalised: C_fg(d) / sqrt(C_ff(0) C_gg(0))
     DET(d)         det of the 3 x 3 matrix C(d); normalised: det of the
@@ -24,6 +26,45 @@ import os
 import numpy as np
 
 NAMES = ("Q", "Q3", "signQ")
+
+
+def multispin_plane_diff(eagb, g, spins, wctb, nrep):
+    """Differing spins per (sample, pair, beta, plane) of multispin
+    configurations (the reference's layout): spins[s] = (even, odd) words of
+    sample s, wctb[s][r][b] the clone of replica r at beta b.  The words are
+    unpacked on the host (ea_host_unpack_replica); pairs (0,1), (2,3), ...
+    Returns diff [nsamples][nrep/2][NB][Lz]."""
+    L, Lz, NB = g.L, g.Lz, g.nbetas
+    ns = len(spins)
+    out = np.zeros((ns, nrep // 2, NB, Lz), np.int32)
+    for s, (even, odd) in enumerate(spins):
+        u = [eagb.host_unpack_replica(g, even, odd, r) for r in range(nrep)]
+        for k in range(nrep // 2):
+            for b in range(NB):
+                a = u[2 * k][wctb[s][2 * k][b]]
+                c = u[2 * k + 1][wctb[s][2 * k + 1][b]]
+                out[s, k, b] = (a != c).reshape(Lz, L * L).sum(1)
+    return out
+
+
+def plane_correlations(diff, L2, pbc, dmax):
+    """The correlation matrices of ea_sp_plane_correlations computed on the
+    host from plane counts diff[sample][pair][beta][z] (numpy summation
+    order): C[sample][beta][d][3][3]."""
+    q = 1.0 - (2.0 / L2) * diff.astype(np.float64)
+    F = np.stack([q, q * q * q, np.sign(q)], -1)            # [s][pair][b][z][3]
+    Lz = diff.shape[-1]
+    ns, _, NB, _ = diff.shape
+    out = np.zeros((ns, NB, dmax + 1, 3, 3))
+    for d in range(dmax + 1):
+        if pbc:
+            A, B = F, np.roll(F, -d, axis=3)
+        else:
+            A, B = F[:, :, :, :Lz - d], F[:, :, :, d:]
+        if A.shape[3] == 0:
+            continue
+        out[:, :, d] = np.einsum("skbzf,skbzg->sbfg", A, B) / (A.shape[1] * A.shape[3])
+    return out
 
 
 def _normalised(M):

@@ -141,6 +141,21 @@ def host_init_spins(g, seed_u):
     return ev, od
 
 
+def host_unpack_replica(g, even, odd, rep):
+    """ea_host_unpack_replica: the spins of every clone of one replica as
+    bytes [NB][V] (0/1), site x + L*y + L*L*z."""
+    half, V = sizes(g)
+    u = np.zeros((g.nbetas, V), np.uint8)
+    _ck(lib().ea_host_unpack_replica(C.byref(g), P(np.ascontiguousarray(even, np.uint64)),
+                                     P(np.ascontiguousarray(odd, np.uint64)), int(rep), P(u)))
+    return u
+
+
+def host_pack_replica(g, u, rep, even, odd):
+    """ea_host_pack_replica: bytes [NB][V] into replica `rep` of the even/odd arrays."""
+    _ck(lib().ea_host_pack_replica(C.byref(g), P(np.ascontiguousarray(u, np.uint8)), int(rep), P(even), P(odd)))
+
+
 def host_init_couplings(g, seed_J):
     half, V = sizes(g)
     J6 = np.zeros(6 * V, np.uint8)

@@ -112,3 +112,36 @@ def test_plane_overlaps_and_correlations(L, Lz, bc, NR, nrep):
     nonzero = (2 * diff != L2).mean(axis=(2, 4)).reshape(64, len(betas))
     assert np.allclose(C[:, :, 0, 2, 2], nonzero)
     job.close()
+
+
+def test_multispin_plane_diff_and_host_correlations():
+    """Multispin configurations (the reference's layout): plane counts from
+    the packed words equal counts from the bytes they were packed from, with
+    each replica's clone at each beta; the host correlations equal the
+    restatement within FP64 rounding (numpy sums in another order)."""
+    L, Lz, NB, NR, ns = 8, 16, 3, 4, 2
+    g = eagb.geom(L, Lz, NB, NR=NR, nsamples=ns, bc=eagb.EA_PBC)
+    half, V = eagb.sizes(g)
+    rng = np.random.default_rng(9)
+    spins, bytes_ = [], []
+    for s in range(ns):
+        even = np.zeros(NB * half * NR, np.uint64)
+        odd = np.zeros(NB * half * NR, np.uint64)
+        u = rng.integers(0, 2, size=(NR, NB, V), dtype=np.uint8)
+        for r in range(NR):
+            eagb.host_pack_replica(g, u[r], r, even, odd)
+        spins.append((even, odd))
+        bytes_.append(u)
+    wctb = np.array([[rng.permutation(NB) for _ in range(NR)] for _ in range(ns)])
+    diff = analysis.multispin_plane_diff(eagb, g, spins, wctb, 4)
+    for s in range(ns):
+        for k in range(2):
+            for b in range(NB):
+                a = bytes_[s][2 * k][wctb[s][2 * k][b]]
+                c = bytes_[s][2 * k + 1][wctb[s][2 * k + 1][b]]
+                assert np.array_equal(diff[s, k, b], (a != c).reshape(Lz, L * L).sum(1))
+    C = analysis.plane_correlations(diff, L * L, True, 5)
+    # the restatement walks 64 lanes of one word: the samples, then zero padding
+    padded = np.concatenate([diff[None], np.zeros((1, 64 - ns, 2, NB, Lz), np.int32)], 1)
+    want = restated_correlations(padded, L * L, Lz, True, 5)[:ns]
+    assert np.allclose(C, want, rtol=1e-12, atol=1e-14)
