@@ -593,31 +593,32 @@ __device__ __forceinline__ uint4 pack8(const uint32_t l[8]) {
   return make_uint4(l[0] | (l[1] << 16), l[2] | (l[3] << 16), l[4] | (l[5] << 16), l[6] | (l[7] << 16));
 }
 
-__device__ __forceinline__ void sp_cluster8_body(const SpDev &d, int g, int blk, unsigned char *sm) {
-  const unsigned long long key = sp_cluster_key(d);
-  const int V = d.V, nc = d.nclust;
-  uint4 *lab = reinterpret_cast<uint4 *>(sm);                                  // [V]: 8 labels
-  uint16_t *lab16 = reinterpret_cast<uint16_t *>(sm);                          // the same, one label each
-  unsigned long long *bond = reinterpret_cast<unsigned long long *>(sm + (size_t)16 * V);  // [V]
-  uint8_t *qb = sm + (size_t)24 * V;                                           // [V] q bits, then coins
-  const int grp = blk & 7, lat = blk >> 3;
-  const int b = lat % nc, w = lat / nc;
-  uint8_t *Qb = reinterpret_cast<uint8_t *>(d.Q + (size_t)lat * V) + grp;
-  for (int i = threadIdx.x; i < V; i += blockDim.x) qb[i] = Qb[(size_t)i * 8];
+// The 8-sample lock-step labelling of the sites [base, base + Vs) (all of
+// the lattice, or one slab of z planes): bonds to sites outside the run are
+// left out; labels are local indices (site - base).  SMEM: lab [Vs] (8
+// labels a site), bond [Vs], qb [Vs] (the group's 8 q bits a site).
+__device__ __forceinline__ void sp_label8(const SpDev &d, const uint8_t *Qb, int base, int Vs, unsigned char *sm) {
+  uint4 *lab = reinterpret_cast<uint4 *>(sm);
+  uint16_t *lab16 = reinterpret_cast<uint16_t *>(sm);
+  unsigned long long *bond = reinterpret_cast<unsigned long long *>(sm + (size_t)16 * Vs);
+  uint8_t *qb = sm + (size_t)24 * Vs;
+  for (int i = threadIdx.x; i < Vs; i += blockDim.x) qb[i] = Qb[(size_t)(base + i) * 8];
   __syncthreads();
-  for (int i = threadIdx.x; i < V; i += blockDim.x) {
+  for (int i = threadIdx.x; i < Vs; i += blockDim.x) {
     const uint32_t qi = qb[i];
+    const int gi = base + i;
     unsigned long long m = 0;
 #pragma unroll
     for (int q = 0; q < 6; ++q) {
-      const int p = __ldg(d.nb + (size_t)i * 6 + q);
-      if (p < i) m |= spread8(~(qi ^ qb[p]) & 0xFFu) << q;
+      const int p = __ldg(d.nb + (size_t)gi * 6 + q);
+      if (p >= base && p < gi) m |= spread8(~(qi ^ qb[p - base]) & 0xFFu) << q;
     }
     bond[i] = m;
     const uint32_t ii = (uint32_t)i | ((uint32_t)i << 16);
     lab[i] = make_uint4(ii, ii, ii, ii);
   }
   __syncthreads();
+  const int V = Vs;
   for (;;) {
     int hooked = 0;
     for (int i = threadIdx.x; i < V; i += blockDim.x) {
@@ -629,7 +630,7 @@ __device__ __forceinline__ void sp_cluster8_body(const SpDev &d, int g, int blk,
       for (int q = 0; q < 6; ++q) {
         const unsigned long long mq = (m >> q) & 0x0101010101010101ull;
         if (!mq) continue;
-        const int p = __ldg(d.nb + (size_t)i * 6 + q);
+        const int p = __ldg(d.nb + (size_t)(base + i) * 6 + q) - base;
         uint32_t lj[8];
         unpack8(lab[p], lj);
 #pragma unroll
@@ -657,6 +658,17 @@ __device__ __forceinline__ void sp_cluster8_body(const SpDev &d, int g, int blk,
       if (!__syncthreads_or(moved)) break;
     }
   }
+}
+
+__device__ __forceinline__ void sp_cluster8_body(const SpDev &d, int g, int blk, unsigned char *sm) {
+  const unsigned long long key = sp_cluster_key(d);
+  const int V = d.V, nc = d.nclust;
+  uint4 *lab = reinterpret_cast<uint4 *>(sm);                                  // [V]: 8 labels
+  uint8_t *qb = sm + (size_t)24 * V;                                           // [V] q bits, then coins
+  const int grp = blk & 7, lat = blk >> 3;
+  const int b = lat % nc, w = lat / nc;
+  uint8_t *Qb = reinterpret_cast<uint8_t *>(d.Q + (size_t)lat * V) + grp;
+  sp_label8(d, Qb, 0, V, sm);
   // coins of the roots (in qb, no longer needed), then the flip bytes
   const unsigned long long mv = *d.move;
   for (int i = threadIdx.x; i < V; i += blockDim.x) {
@@ -683,6 +695,89 @@ __device__ __forceinline__ void sp_cluster8_body(const SpDev &d, int g, int blk,
     for (int l = 0; l < 8; ++l) f |= ((uint32_t)(qb[x[l]] >> l) & 1u) << l;
     Qb[(size_t)i * 8] = (uint8_t)f;
   }
+}
+
+// ---------------------------------------------------------------------------
+// Lattices above kSpClusterMaxV sites, one-job path: slabs of slabD z planes
+// labelled 8 samples at a time in SMEM (sp_label8), each site's label written
+// as a global site index into slab_lab [unit = lattice * 8 + group][8][V];
+// then the bonds between slabs joined by the lock-free union of the
+// multispin path (cc_unite: a root hung below the smaller one with
+// atomicMin), the labels compressed to their roots and the roots' coins
+// drawn (slab_coin [unit][V], one bit a sample), and the flip bytes written
+// in place of the overlap bytes.  Labels only decrease and never drop below
+// the smallest site of their cluster, so the roots -- and the coins and
+// flips -- are those of the one-CTA labelling.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void sp_slab8_body(const SpDev &d, int unit, int sl, unsigned char *sm) {
+  const int V = d.V, L2 = d.L * d.L, z0 = sl * d.slabD;
+  const int base = z0 * L2, Vs = min(d.slabD, d.Lz - z0) * L2;
+  const int grp = unit & 7, lat = unit >> 3;
+  const uint8_t *Qb = reinterpret_cast<const uint8_t *>(d.Q + (size_t)lat * V) + grp;
+  sp_label8(d, Qb, base, Vs, sm);
+  const uint4 *lab = reinterpret_cast<const uint4 *>(sm);
+  uint32_t *Lu = d.slab_lab + (size_t)unit * 8 * V;
+  for (int i = threadIdx.x; i < Vs; i += blockDim.x) {
+    uint32_t x[8];
+    unpack8(lab[i], x);
+#pragma unroll
+    for (int l = 0; l < 8; ++l) Lu[(size_t)l * V + base + i] = (uint32_t)(base + (int)x[l]);
+  }
+}
+
+// Bonds between slabs (each once, from its larger end): t = unit * V + site.
+__device__ __forceinline__ void sp_slab_merge_body(const SpDev &d, long long t) {
+  const int V = d.V, L2 = d.L * d.L;
+  if (t >= (long long)d.nw * d.nclust * 8 * V) return;
+  const int unit = (int)(t / V), gi = (int)(t - (long long)unit * V);
+  const int grp = unit & 7, lat = unit >> 3;
+  const uint8_t *Qb = reinterpret_cast<const uint8_t *>(d.Q + (size_t)lat * V) + grp;
+  const int s1 = gi / L2 / d.slabD;
+  const uint32_t qi = Qb[(size_t)gi * 8];
+  uint32_t *Lu = d.slab_lab + (size_t)unit * 8 * V;
+#pragma unroll
+  for (int q = 0; q < 6; ++q) {
+    const int p = __ldg(d.nb + (size_t)gi * 6 + q);
+    if (p >= gi || p / L2 / d.slabD == s1) continue;
+    const uint32_t eq = ~(qi ^ Qb[(size_t)p * 8]) & 0xFFu;
+    for (int l = 0; l < 8; ++l)
+      if ((eq >> l) & 1u) cc_unite(Lu + (size_t)l * V, (uint32_t)gi, (uint32_t)p);
+  }
+}
+
+// Roots and their coins: t = unit * V + site.
+__device__ __forceinline__ void sp_slab_roots_body(const SpDev &d, int g, long long t) {
+  const int V = d.V, nc = d.nclust;
+  if (t >= (long long)d.nw * nc * 8 * V) return;
+  const int unit = (int)(t / V), gi = (int)(t - (long long)unit * V);
+  const int grp = unit & 7, lat = unit >> 3, b = lat % nc, w = lat / nc;
+  const unsigned long long key = sp_cluster_key(d), mv = *d.move;
+  uint32_t *Lu = d.slab_lab + (size_t)unit * 8 * V;
+  uint32_t coins = 0;
+  for (int l = 0; l < 8; ++l) {
+    const uint32_t r = cc_find(Lu + (size_t)l * V, (uint32_t)gi);
+    Lu[(size_t)l * V + gi] = r;
+    if (r != (uint32_t)gi) continue;
+    const int lane = grp * 8 + l;
+    const uint32_t tag = (((uint32_t)(w * 64 + lane) << 6 | (uint32_t)b) << 1) | (uint32_t)g;
+    uint32_t v0 = (uint32_t)mv, v1 = (uint32_t)(mv >> 32), v2 = (uint32_t)gi, v3 = tag;
+    philox10(v0, v1, v2, v3, (uint32_t)key, (uint32_t)(key >> 32));
+    coins |= (v0 & 1u) << l;
+  }
+  d.slab_coin[(size_t)unit * V + gi] = (uint8_t)coins;
+}
+
+// Flip bytes from the roots' coins, in place of the overlap bytes.
+__device__ __forceinline__ void sp_slab_flip_body(const SpDev &d, long long t) {
+  const int V = d.V;
+  if (t >= (long long)d.nw * d.nclust * 8 * V) return;
+  const int unit = (int)(t / V), gi = (int)(t - (long long)unit * V);
+  const int grp = unit & 7, lat = unit >> 3;
+  const uint32_t *Lu = d.slab_lab + (size_t)unit * 8 * V;
+  const uint8_t *Cu = d.slab_coin + (size_t)unit * V;
+  uint32_t f = 0;
+  for (int l = 0; l < 8; ++l) f |= (uint32_t)((Cu[Lu[(size_t)l * V + gi]] >> l) & 1u) << l;
+  reinterpret_cast<uint8_t *>(d.Q + (size_t)lat * V)[(size_t)gi * 8 + grp] = (uint8_t)f;
 }
 
 // Labelling of one CTA's (word, slot, 8 samples) by lattice size.
@@ -1154,6 +1249,19 @@ __global__ void __launch_bounds__(1024, 1) k_sp_cluster(const __grid_constant__ 
   extern __shared__ __align__(16) uint32_t sm[];
   sp_cluster_any(d, g, blockIdx.x, reinterpret_cast<unsigned char *>(sm));
 }
+__global__ void __launch_bounds__(1024, 1) k_sp_slab8(const __grid_constant__ SpDev d) {
+  extern __shared__ __align__(16) unsigned char sm8[];
+  sp_slab8_body(d, blockIdx.y, blockIdx.x, sm8);
+}
+__global__ void k_sp_slab_merge(const __grid_constant__ SpDev d) {
+  sp_slab_merge_body(d, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
+__global__ void k_sp_slab_roots(const __grid_constant__ SpDev d, int g) {
+  sp_slab_roots_body(d, g, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
+__global__ void k_sp_slab_flip(const __grid_constant__ SpDev d) {
+  sp_slab_flip_body(d, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
 __global__ void k_sp_flip(const __grid_constant__ SpDev d, int g) {
   sp_flip_body(d, g, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
@@ -1193,6 +1301,8 @@ cudaError_t sp_setup() {
                                            std::max(sp_cluster_smem(kSpCluster4MaxV), sp_cluster_smem(kSpCluster8MaxV))));
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_sp_permute, cudaFuncAttributeMaxDynamicSharedMemorySize, kPermRows * 65 * 8);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_sp_slab8, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp_cluster_smem(kSpCluster8MaxV));
   return e;
 }
 
@@ -1236,13 +1346,33 @@ size_t sp_cluster_smem(int V) {
 // same as 1024).
 int sp_cluster_threads(int V) { return V <= 2048 ? 256 : 1024; }
 
+// Planes per slab of the slab labelling of lattices above kSpClusterMaxV
+// sites: as many whole planes as the 8-sample SMEM labelling takes; 0 (the
+// one-CTA labelling in global scratch) when a plane alone is too large or
+// the labels of every (word, slot, group) would pass 4 GB.
+int sp_slab_planes(int L, int Lz, int nw, int nclust) {
+  const long long L2 = (long long)L * L, V = L2 * Lz;
+  if (V <= kSpClusterMaxV || L2 > kSpCluster8MaxV) return 0;
+  if ((long long)nw * nclust * 8 * V * 33 > (4ll << 30)) return 0;
+  return (int)std::min<long long>(Lz, kSpCluster8MaxV / L2);
+}
+
 cudaError_t sp_launch_houdayer(const SpDev &d, cudaStream_t st) {
   k_sp_pairs<<<1, 32, 0, st>>>(d);
   const int ng = d.NR >= 4 ? 2 : 1;
   for (int g = 0; g < ng; ++g) {
     const long long n = (long long)d.nw * d.nclust * d.V;
     k_sp_overlap<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d, g);
-    k_sp_cluster<<<(unsigned)(d.nw * d.nclust * 8), d.cthreads, sp_cluster_smem(d.V), st>>>(d, g);
+    if (d.slabD > 0) {
+      const int L2 = d.L * d.L, nslab = (d.Lz + d.slabD - 1) / d.slabD, nunits = d.nw * d.nclust * 8;
+      const long long nu = (long long)nunits * d.V;
+      k_sp_slab8<<<dim3((unsigned)nslab, (unsigned)nunits), 1024, sp_cluster_smem(d.slabD * L2), st>>>(d);
+      k_sp_slab_merge<<<(unsigned)((nu + 255) / 256), 256, 0, st>>>(d);
+      k_sp_slab_roots<<<(unsigned)((nu + 255) / 256), 256, 0, st>>>(d, g);
+      k_sp_slab_flip<<<(unsigned)((nu + 255) / 256), 256, 0, st>>>(d);
+    } else {
+      k_sp_cluster<<<(unsigned)(d.nw * d.nclust * 8), d.cthreads, sp_cluster_smem(d.V), st>>>(d, g);
+    }
     k_sp_flip<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d, g);
   }
   return cudaGetLastError();
@@ -1439,6 +1569,8 @@ int ea_sp_destroy(ea_sp *c) {
   if (c->d.dos) cudaFree(c->d.dos);
   if (c->d.Q) cudaFree(c->d.Q);
   if (c->d.cscratch) cudaFree(c->d.cscratch);
+  if (c->d.slab_lab) cudaFree(c->d.slab_lab);
+  if (c->d.slab_coin) cudaFree(c->d.slab_coin);
   if (c->it_graph) cudaGraphExecDestroy(c->it_graph);
   if (c->p_jobs) cudaFree(c->p_jobs);
   if (c->p_pre) cudaFree(c->p_pre);
@@ -1813,11 +1945,24 @@ static int sp_cluster_prepare(ea_sp *c, int &nclust) {
     SCU(cudaStreamSynchronize(c->st));
     if (d.Q) cudaFree(d.Q);
     if (d.cscratch) cudaFree(d.cscratch);
+    if (d.slab_lab) cudaFree(d.slab_lab);
+    if (d.slab_coin) cudaFree(d.slab_coin);
     d.Q = nullptr;
     d.cscratch = nullptr;
+    d.slab_lab = nullptr;
+    d.slab_coin = nullptr;
+    d.slabD = 0;
     SCU(cudaMalloc((void **)&d.Q, sizeof(unsigned long long) * (size_t)d.nw * nclust * d.V));
-    if (d.V > kSpClusterMaxV)
+    if (d.V > kSpClusterMaxV) {
       SCU(cudaMalloc((void **)&d.cscratch, sizeof(uint32_t) * sp_cluster_words(d.V) * (size_t)d.nw * nclust * 8));
+      const int D = sp_slab_planes(d.L, d.Lz, d.nw, nclust);
+      if (D > 0) {
+        const size_t units = (size_t)d.nw * nclust * 8;
+        SCU(cudaMalloc((void **)&d.slab_lab, sizeof(uint32_t) * units * 8 * d.V));
+        SCU(cudaMalloc((void **)&d.slab_coin, units * d.V));
+        d.slabD = D;
+      }
+    }
     c->q_cap = nclust;
   }
   d.nclust = nclust;
@@ -2358,6 +2503,10 @@ int ea_sp_job_bytes(const ea_sp_geom *gp, const ea_cadence *cad, const double *b
     const uint64_t nc = (uint64_t)(cad->nclust > 0 ? std::min<int>(cad->nclust, (int)NB) : std::lround(0.5 * NB));
     add(nw * nc * V * 8);
     if (V > (uint64_t)kSpClusterMaxV) add(nw * nc * 8 * sp_cluster_words((int)V) * 4);
+    if (sp_slab_planes(gp->L, gp->Lz, (int)nw, (int)nc) > 0) {   // slab labels and coins
+      add(nw * nc * 8 * 8 * V * 4);
+      add(nw * nc * 8 * V);
+    }
   }
   if (cad && sp_res_fits(gp->L, gp->Lz, (int)nw, (int)NR, (int)NB)) {
     // the resident kernel's counters, random words and tempering uniforms

@@ -72,6 +72,9 @@ struct SpDev {
   unsigned long long *move;          // cluster moves so far
   int nclust;
   uint32_t *cscratch;                // labelling arrays of lattices above kSpClusterMaxV, per CTA
+  int slabD;                         // > 0: such lattices labelled in slabs of slabD z planes (one-job path)
+  uint32_t *slab_lab;                // [nw*nclust*8 units][8][V] labels of the slab path
+  uint8_t *slab_coin;                // [units][V] roots' coins (one bit a sample)
   // exact enumeration
   unsigned long long *dos;           // [nw][64][6V+1] states per energy (E = -3V..3V)
 };
@@ -86,6 +89,7 @@ constexpr int kSpCluster4MaxV = 10500;
 __host__ __device__ inline size_t sp_cluster_words(int V) { return ((size_t)V * 7 + 15) / 16 * 4; }
 
 int sp_kt(int NB, int NR, int nsites_colour);
+int sp_slab_planes(int L, int Lz, int nw, int nclust);
 int sp_energy_chunk(const SpDev &d);
 size_t sp_sweep_smem(int NB, int NR, int kt);
 cudaError_t sp_setup();

@@ -271,10 +271,13 @@ def test_sweeps_energy_tempering_match_oracle(L, Lz, bc, ln, NR, nw):
 @pytest.mark.gpu
 # lattices of the four labelling paths: up to 8900 sites all 8 samples per
 # pass (odd and even L, PBC and OBC), up to 10500 4 samples per pass, up to
-# 32768 one sample at a time in SMEM, above in global scratch
+# 32768 one sample at a time in SMEM, above in slabs of z planes joined by a
+# union across the slab faces (odd L OBC: corner fake bonds between the two
+# open planes; even L PBC: the z wrap)
 @pytest.mark.parametrize("L,Lz,bc,NR,nw", [(5, 6, eagb.EA_OBC, 4, 2), (3, 3, eagb.EA_PBC, 2, 1), (4, 8, eagb.EA_OBC, 8, 1),
                                            (2, 5, eagb.EA_OBC, 2, 1), (10, 96, eagb.EA_OBC, 2, 1),
-                                           (11, 90, eagb.EA_PBC, 2, 1), (19, 96, eagb.EA_OBC, 2, 1)])
+                                           (11, 90, eagb.EA_PBC, 2, 1), (19, 96, eagb.EA_OBC, 2, 1),
+                                           (16, 130, eagb.EA_PBC, 4, 1)])
 def test_houdayer_matches_oracle(L, Lz, bc, NR, nw):
     job = new_job(L, Lz, bc, "T07_16_N6", NR, nw)
     orc = OracleSP(job, 3)
