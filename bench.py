@@ -97,11 +97,51 @@ def lut_search_iters(cum):
     return tot / float(1 << 64)
 
 
-def int_ops(cums, triples, words):
+def lut_search_iters11(cum):
+    """The same expectation for the 11-bit pre-search of the per-item pass
+    (lut_byte11): bucket t = R >> 53 searches [pre[t], pre[t+1]], pre[t] the
+    first byte whose threshold is above t << 53."""
+    c = [int(x) for x in np.asarray(cum, np.uint64)]
+
+    def first_above(R):
+        lo, hi = 0, 255
+        while lo < hi:
+            m = (lo + hi) >> 1
+            if R < c[m]:
+                hi = m
+            else:
+                lo = m + 1
+        return lo
+
+    pre = [first_above(t << 53) for t in range(2048)] + [255]
+    tot = 0
+    for t in range(2048):
+        a0, b0 = pre[t], pre[t + 1]
+        if a0 == b0:
+            continue
+        lo_r, hi_r = t << 53, ((t + 1) << 53) - 1
+        for n in range(a0, b0 + 1):
+            lo = max(c[n - 1] if n > 0 else 0, lo_r)
+            hi = hi_r if n == 255 else min(c[n] - 1, hi_r)
+            if hi < lo:
+                continue
+            a, b, d = a0, b0, 0
+            while a < b:
+                m = (a + b) >> 1
+                d += 1
+                if n <= m:
+                    b = m
+                else:
+                    a = m + 1
+            tot += (hi - lo + 1) * d
+    return tot / float(1 << 64)
+
+
+def int_ops(cums, triples, words, iters=lut_search_iters):
     """32-bit integer operations of a launch that draws `triples` random
     triples (spread evenly over the temperatures of `cums`) and updates
     `words` spin words."""
-    e = float(np.mean([lut_search_iters(c) for c in cums]))
+    e = float(np.mean([iters(c) for c in cums]))
     return triples * (OPS_TRIPLE_BASE + OPS_PER_ITER * e) + words * OPS_WORD, e
 
 
@@ -520,12 +560,21 @@ def run_sp(args, dev, torch, eagb):
                 job.run_async(**cad)
             t1.record(st)
             job.sync()
+            ms = t0.elapsed_time(t1)
             ncol, kt = job.info()
             S = job.get_spins()
+            if form != "resident":
+                # the colour passes alone (counter fills + passes of 20 sweeps)
+                t0.record(st)
+                job.sweeps(20)
+                t1.record(st)
+                job.sync()
+                pass_us[0] = 1e3 * t0.elapsed_time(t1) / 20
             job.close()
-            return t0.elapsed_time(t1), form, ncol, kt, S
+            return ms, form, ncol, kt, S
 
         tuned = [0, 0, 0]
+        pass_us = [0.0]
         ms, form, ncol, kt, S = timed(eagb.EA_BIN_AUTO)
         V = Lx * Lx * Lz
         sweeps = steps * itmax * houfr * ptfr
@@ -535,6 +584,25 @@ def run_sp(args, dev, torch, eagb):
                "samples": 64 * nw, "bin_kernel": form, "l2": "job of %.1f MB" % (V * NR * len(d["betas"]) * nw * 8 / 1e6)}
         if form != "resident":
             rec["autotuned"] = {"tile": tuned[0], "energy_sites_per_thread": tuned[1], "labelling_threads": tuned[2]}
+            # roofline of the colour passes of one sweep: 24 B per spin word
+            # (read + write it, read it once as a neighbour) + 48 B of
+            # couplings per (site, sample word); integer ops of the random
+            # triples (one per site, replica and slot, shared by the words)
+            # and the word updates, the search iterations of the pass's
+            # pre-search (11 bits for the per-item pass, 8 for tiles)
+            hbm, _ = peaks()
+            ipk_alu, _ = int_peak(eagb, dev)
+            words = V * NR * len(d["betas"]) * nw
+            pbytes = words * 24 + V * nw * 48
+            ops, e_it = int_ops(d["cum"], V * NR * len(d["betas"]), words,
+                                lut_search_iters11 if kt == 0 else lut_search_iters)
+            hf = pbytes / (pass_us[0] * 1e-6) / 1e9 / hbm
+            inf = ops / (pass_us[0] * 1e-6) / ipk_alu
+            rec["pass"] = {"form": "per-item" if kt == 0 else "tiles of %d sites" % kt,
+                           "us_per_sweep": pass_us[0], "bound": "int32" if inf > hf else "hbm",
+                           "frac": max(hf, inf), "hbm_frac": hf, "int_frac": inf,
+                           "alg_bytes_per_sweep": pbytes, "int_ops_per_sweep": ops,
+                           "search_iterations_per_byte": e_it}
         if form == "resident":
             # the same bins as a graph of per-phase launches, from the same start
             gms, _, _, _, gS = timed(eagb.EA_BIN_GRAPH)

@@ -304,6 +304,21 @@ void presearch8(const uint64_t *cum, uint16_t *pre) {
   }
 }
 
+// The 11-bit pre-search: pre[t] = the first byte n with (t << 53) < cum[n]
+// for t < 2048 and 255 from entry 2048 on (kPre11Stride entries a
+// temperature).  A key R in bucket t = R >> 53 has its byte in
+// [pre[t], pre[t+1]]: the search is monotone in R, so the first byte of the
+// next bucket bounds every byte of this one.
+void presearch11(const uint64_t *cum, uint8_t *pre) {
+  int n = 0;
+  for (int t = 0; t < 2048; ++t) {
+    const uint64_t lo = (uint64_t)t << 53;
+    while (n < 255 && !(lo < cum[n])) ++n;
+    pre[t] = (uint8_t)n;
+  }
+  for (int t = 2048; t < kPre11Stride; ++t) pre[t] = 255;
+}
+
 // pt = -(beta[i+1]-beta[i]) * dE in double, exactly as upd.c:16-17 forms it,
 // and exp() from the host libm, as upd.c:29 calls it.  dE is even (E = 3V - 2n).
 void pt_exp_table(const double *betas, int NB, std::vector<double> &vals, std::vector<int32_t> &offsets) {

@@ -63,6 +63,8 @@ int scalar_energy(const Geometry &g, const uint8_t *u, const uint8_t *J6);
 // 8-bit pre-search of the cumulative thresholds: entry b = (lo, hi) bounds of the
 // byte drawn for any R whose top 8 bits are b.
 void presearch8(const uint64_t *cum, uint16_t *pre);
+constexpr int kPre11Stride = 2064;  // 2049 entries a temperature, padded to 16 bytes
+void presearch11(const uint64_t *cum, uint8_t *pre);
 
 // glibc exp() of every parallel-tempering exponent that can change a decision,
 // laid out per beta pair: offsets[i] .. offsets[i+1] hold exp(pt) for

@@ -95,9 +95,27 @@ __device__ __forceinline__ uint32_t lut_byte(uint32_t hi, uint32_t lo, const u64
   return a;
 }
 
-template <bool GCUM = false>
-__device__ __forceinline__ uint32_t rnd_word(uint32_t cx, uint32_t cy, uint32_t cz, uint32_t cw, uint32_t key,
-                                             uint32_t tid, const u64 *cum, const uint16_t *pre) {
+// The same search with the 11-bit pre-search of presearch11 (host.cpp): a
+// key in bucket t = hi >> 21 has its byte in [pre[t], pre[t+1]]; thresholds
+// through the read-only cache.  Narrower buckets leave a bisection to fewer
+// keys: 0.04 steps per byte on the benchmark sets against 0.18-0.21 with the
+// 8-bit pre-search, and a warp waits for its slowest lane at each search.
+__device__ __forceinline__ uint32_t lut_byte11(uint32_t hi, uint32_t lo, const u64 *cum, const uint8_t *pre) {
+  const u64 R = ((u64)hi << 32) | lo;
+  const uint32_t t = hi >> 21;
+  uint32_t a = pre[t], b = pre[t + 1];
+  while (a < b) {
+    const uint32_t m = (a + b) >> 1;
+    if (R < __ldg(cum + m)) b = m; else a = m + 1;
+  }
+  return a;
+}
+
+// One random word from a Philox counter: the four keys' bytes by `byte`
+// (a threshold search), rotated as the post-mix says.
+template <class Byte>
+__device__ __forceinline__ uint32_t rnd_word_by(uint32_t cx, uint32_t cy, uint32_t cz, uint32_t cw, uint32_t key,
+                                                uint32_t tid, Byte byte) {
   uint32_t v0 = cx, v1 = cy, v2 = cz, v3 = cw;
   philox10(v0, v1, v2, v3, tid, key);
   const uint32_t h = v0 ^ v2, l = v1 ^ v3;
@@ -106,9 +124,15 @@ __device__ __forceinline__ uint32_t rnd_word(uint32_t cx, uint32_t cy, uint32_t 
   const uint32_t s2 = __funnelshift_l(l, h, 28);
   const uint32_t s3 = __funnelshift_l(h, l, 28);
   const uint32_t rot = (s0 + v1 + s2 + v3) >> 27;
-  const uint32_t bb = lut_byte<GCUM>(v0, s0, cum, pre) | (lut_byte<GCUM>(v1, s1, cum, pre) << 8) |
-                      (lut_byte<GCUM>(v2, s2, cum, pre) << 16) | (lut_byte<GCUM>(v3, s3, cum, pre) << 24);
+  const uint32_t bb = byte(v0, s0) | (byte(v1, s1) << 8) | (byte(v2, s2) << 16) | (byte(v3, s3) << 24);
   return __funnelshift_l(bb, bb, rot);  // rotate left; rot 0 leaves the word as it is
+}
+
+template <bool GCUM = false>
+__device__ __forceinline__ uint32_t rnd_word(uint32_t cx, uint32_t cy, uint32_t cz, uint32_t cw, uint32_t key,
+                                             uint32_t tid, const u64 *cum, const uint16_t *pre) {
+  return rnd_word_by(cx, cy, cz, cw, key, tid,
+                     [&](uint32_t hi, uint32_t lo) { return lut_byte<GCUM>(hi, lo, cum, pre); });
 }
 
 // ---------------------------------------------------------------------------

@@ -1231,6 +1231,59 @@ __global__ void __launch_bounds__(512) k_sp_pass(const __grid_constant__ SpDev d
   extern __shared__ __align__(16) unsigned char smem[];
   sp_pass_body(d, off, n, blockIdx.x, smem);
 }
+
+// One colour pass as a persistent grid of per-item threads: a thread takes
+// (site, replica, slot) items of the colour in turn -- consecutive lanes on
+// consecutive slots, so a warp's loads and stores cover consecutive words --
+// draws the item's three random words and updates the item's word in each
+// sample word.  Each CTA stages the 11-bit pre-search tables once (the
+// thresholds, rarely read past them, come through the read-only cache); no
+// random word goes through SMEM and no barrier separates drawing from
+// updating.  Same words as k_sp_pass (same random words per (slot, site,
+// replica), same flip mask): this form suits jobs with few sample words,
+// whose staged tiles spend their time on barriers and SMEM traffic for words
+// used once.
+__global__ void __launch_bounds__(512) k_sp_pass_items(const __grid_constant__ SpDev d, int off, int n) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int NB = d.NB, NR = d.NR, G = NR * NB, V = d.V;
+  uint8_t *s_pre = smem;
+  {
+    const uint4 *ps = reinterpret_cast<const uint4 *>(d.pre11);
+    uint4 *pd = reinterpret_cast<uint4 *>(s_pre);
+    for (int i = threadIdx.x; i < NB * (kPre11Stride / 16); i += blockDim.x) pd[i] = ps[i];
+  }
+  __syncthreads();
+  const long long total = (long long)n * G, stride = (long long)gridDim.x * blockDim.x;
+  const size_t wps = (size_t)V * G;  // words per sample word
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
+    const int b = (int)(t % NB), r = (int)((t / NB) % NR), k = (int)(t / G);
+    const int site = __ldg(d.col_sites + off + k);
+    const uint32_t tp = (uint32_t)(((size_t)b * V + site) * NR + r);
+    const uint4 c = d.ctr[r];
+    const uint32_t key = __ldg(d.keys + r);
+    const u64 *cum = d.cum + b * 256;
+    const uint8_t *pre = s_pre + b * kPre11Stride;
+    uint32_t w[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q)
+      w[q] = rnd_word_by(c.x + q, c.y, c.z + tp, c.w, key, tp,
+                         [&](uint32_t hi, uint32_t lo) { return lut_byte11(hi, lo, cum, pre); });
+    const u64 r0 = ((u64)w[0] << 32) | w[1], r1 = ((u64)w[2] << 32) | w[3], r2 = ((u64)w[4] << 32) | w[5];
+    int nbr[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) nbr[q] = __ldg(d.nb + (size_t)site * 6 + q);
+    u64 *Sc = d.S + (size_t)r * NB + b;
+    for (int ww = 0; ww < d.nw; ++ww) {
+      u64 *Sw = Sc + (size_t)ww * wps;
+      const u64 *Jp = d.J + ((size_t)ww * V + site) * 6;
+      const u64 sv = Sw[(size_t)site * G];
+      u64 f[6];
+#pragma unroll
+      for (int q = 0; q < 6; ++q) f[q] = sv ^ __ldg(Jp + q) ^ Sw[(size_t)nbr[q] * G];
+      Sw[(size_t)site * G] = sv ^ flip_mask(f, r0, r1, r2);
+    }
+  }
+}
 __global__ void __launch_bounds__(256) k_sp_energy(const __grid_constant__ SpDev d) {
   sp_energy_body(d, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
@@ -1277,6 +1330,17 @@ size_t sp_cluster_smem(int V);
 size_t sp_sweep_smem(int NB, int NR, int kt) {
   return (size_t)NB * 256 * 10 + (size_t)3 * NB * kt * NR * 8 + (size_t)kt * 7 * 4;
 }
+size_t sp_items_smem(int NB) { return (size_t)NB * kPre11Stride; }
+
+// Grid of the per-item pass: every CTA resident at once (the kernel's
+// registers and the threshold tables' SMEM allowing); 0 if none fits.
+int sp_items_grid(int NB) {
+  int dev = 0, nsm = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sp_pass_items, 512, sp_items_smem(NB)) != cudaSuccess)
+    return 0;
+  return per_sm * nsm;
+}
 
 // Tile width: the smallest power of two whose random triples (NB x kt x NR)
 // fill half of the CTA's 512 threads -- narrower tiles leave the CTA staging
@@ -1295,6 +1359,7 @@ int sp_kt(int NB, int NR, int nsites_colour) {
 
 cudaError_t sp_setup() {
   cudaError_t e = cudaFuncSetAttribute(k_sp_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sp_pass_items, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_sp_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)std::max(sp_cluster_smem(kSpClusterMaxV),
@@ -1309,7 +1374,10 @@ cudaError_t sp_setup() {
 cudaError_t sp_launch_pass(const SpDev &d, int colour, int off, int n, cudaStream_t st) {
   k_sp_fill<<<1, 64, 0, st>>>(d);
   (void)colour;
-  if (n > 0) {
+  if (n > 0 && d.pgrid > 0) {
+    const long long blocks = ((long long)n * d.NR * d.NB + 511) / 512;
+    k_sp_pass_items<<<(unsigned)std::min<long long>(blocks, d.pgrid), 512, sp_items_smem(d.NB), st>>>(d, off, n);
+  } else if (n > 0) {
     const int grid = (n + d.kt - 1) / d.kt;
     k_sp_pass<<<grid, 512, sp_sweep_smem(d.NB, d.NR, d.kt), st>>>(d, off, n);
   }
@@ -1531,6 +1599,7 @@ int ea_sp_create(const ea_sp_geom *gp, int32_t device, ea_sp **out) {
   { unsigned long long *p; SOWN(p, nw * V * 6); d.J = p; }
   { unsigned long long *p; SOWN(p, (size_t)d.NB * 256); d.cum = p; }
   { uint16_t *p; SOWN(p, (size_t)d.NB * 256); d.pre = p; }
+  { uint8_t *p; SOWN(p, (size_t)d.NB * kPre11Stride); d.pre11 = p; }
   SOWN(d.ctr, (size_t)d.NR);
   { uint32_t *p; SOWN(p, (size_t)d.NR); d.keys = p; }
   SOWN(d.prc, (size_t)d.NR);
@@ -1556,6 +1625,10 @@ int ea_sp_create(const ea_sp_geom *gp, int32_t device, ea_sp **out) {
   for (size_t i = 0; i < perm.size(); ++i) perm[i] = (uint8_t)(i % d.NB);
   SCU(cudaMemcpyAsync(d.perm, perm.data(), perm.size(), cudaMemcpyHostToDevice, c->st));
   SCU(cudaStreamSynchronize(c->st));
+  // one-word jobs take the per-item pass: measured faster than every tile
+  // width on one word (L=6 to 24, 12 to 32 temperatures); many words share
+  // each tile's random words and keep the tiles
+  if (nw == 1) d.pgrid = sp_items_grid(d.NB);
   *out = c;
   return EA_OK;
 }
@@ -1597,7 +1670,7 @@ int ea_sp_device_view(ea_sp *c, SpDev *d, cudaStream_t *st) {
 int ea_sp_info(const ea_sp *c, int32_t *ncol, int32_t *tile) {
   if (!c) return spfail(EA_ERR_ARG, "null job");
   if (ncol) *ncol = c->d.ncol;
-  if (tile) *tile = c->d.kt;
+  if (tile) *tile = c->d.pgrid ? 0 : c->d.kt;
   return EA_OK;
 }
 
@@ -1627,6 +1700,23 @@ int ea_sp_sync(ea_sp *c) {
   return sp_check_persist(c->p_err, c->st);
 }
 
+int ea_sp_set_tile(ea_sp *c, int32_t tile) {
+  if (!c) return spfail(EA_ERR_ARG, "null job");
+  SCU(cudaSetDevice(c->device));
+  SpDev &d = c->d;
+  if (tile == 0) {
+    const int pg = sp_items_grid(d.NB);
+    if (!pg) return spfail(EA_ERR_ARG, "the per-item pass does not fit NB=%d", d.NB);
+    d.pgrid = pg;
+    return EA_OK;
+  }
+  if (tile < 1 || tile > 64 || sp_sweep_smem(d.NB, d.NR, tile) > 227 * 1024 - 512)
+    return spfail(EA_ERR_ARG, "tile %d: 1..64 sites whose tables fit in shared memory", tile);
+  d.kt = tile;
+  d.pgrid = 0;
+  return EA_OK;
+}
+
 int ea_sp_set_bin_kernel(ea_sp *c, int32_t mode) {
   if (!c || mode < EA_BIN_AUTO || mode > EA_BIN_RESIDENT) return spfail(EA_ERR_ARG, "bad bin-kernel mode");
   c->bin_mode = mode;
@@ -1639,9 +1729,11 @@ int ea_sp_set_temperatures(ea_sp *c, const double *betas, const uint64_t *cum) {
   for (int i = 0; i + 1 < NB; ++i)
     if (betas[i] < betas[i + 1]) return spfail(EA_ERR_ARG, "betas must be sorted from largest to smallest");
   std::vector<uint16_t> pre((size_t)NB * 256);
+  std::vector<uint8_t> pre11((size_t)NB * kPre11Stride);
   for (int b = 0; b < NB; ++b) {
     if (cum[(size_t)b * 256 + 255] != ~0ULL) return spfail(EA_ERR_ARG, "threshold 255 of beta %d is not 2^64-1", b);
     presearch8(cum + (size_t)b * 256, pre.data() + (size_t)b * 256);
+    presearch11(cum + (size_t)b * 256, pre11.data() + (size_t)b * kPre11Stride);
   }
   std::vector<double> tab;
   pt_exp_table(betas, NB, tab, c->expoff);
@@ -1653,6 +1745,7 @@ int ea_sp_set_temperatures(ea_sp *c, const double *betas, const uint64_t *cum) {
   SCU(cudaMemcpyAsync(c->exptab, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice, c->st));
   SCU(cudaMemcpyAsync((void *)c->d.cum, cum, sizeof(uint64_t) * 256 * NB, cudaMemcpyHostToDevice, c->st));
   SCU(cudaMemcpyAsync((void *)c->d.pre, pre.data(), pre.size() * 2, cudaMemcpyHostToDevice, c->st));
+  SCU(cudaMemcpyAsync((void *)c->d.pre11, pre11.data(), pre11.size(), cudaMemcpyHostToDevice, c->st));
   SCU(cudaMemcpyAsync((void *)c->d.betas, betas, sizeof(double) * NB, cudaMemcpyHostToDevice, c->st));
   SCU(cudaMemcpyAsync((void *)c->d.expoff, c->expoff.data(), sizeof(int32_t) * NB, cudaMemcpyHostToDevice, c->st));
   SCU(cudaStreamSynchronize(c->st));
@@ -1825,18 +1918,26 @@ int ea_sp_autotune(ea_sp *c, int32_t *tile, int32_t *echunk, int32_t *cthreads) 
   };
   int maxc = 0;
   for (int k = 0; k < d.ncol; ++k) maxc = std::max(maxc, d.col_off[k + 1] - d.col_off[k]);
-  // tile width: the heuristic's and its neighbours that fit in SMEM
-  const int kt0 = d.kt;
-  int best_kt = kt0;
+  // colour pass: the heuristic's tile width and its neighbours that fit in
+  // SMEM, and the per-item pass
+  const int kt0 = d.kt, pg0 = d.pgrid;
+  int best_kt = kt0, best_pg = pg0;
   float best = 1e30f;
+  d.pgrid = 0;
   for (int kt : {kt0 / 2, kt0, kt0 * 2, kt0 * 4}) {
     if (kt < 1 || kt > 64 || sp_sweep_smem(d.NB, d.NR, kt) > 227 * 1024 - 512) continue;
     if ((maxc + kt - 1) / kt < 1) continue;
     d.kt = kt;
     const float ms = timed([&] { sp_sweeps(c, 2); });
-    if (ms < best) { best = ms; best_kt = kt; }
+    if (ms < best) { best = ms; best_kt = kt; best_pg = 0; }
   }
   d.kt = best_kt;
+  if (const int pg = sp_items_grid(d.NB)) {
+    d.pgrid = pg;
+    const float ms = timed([&] { sp_sweeps(c, 2); });
+    if (ms < best) { best = ms; best_pg = pg; }
+  }
+  d.pgrid = best_pg;
   // sites per thread of the energy count
   const int ec0 = d.echunk;
   int best_ec = ec0;
@@ -1875,7 +1976,7 @@ int ea_sp_autotune(ea_sp *c, int32_t *tile, int32_t *echunk, int32_t *cthreads) 
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   SCU(e);
-  if (tile) *tile = d.kt;
+  if (tile) *tile = d.pgrid ? 0 : d.kt;
   if (echunk) *echunk = d.echunk;
   if (cthreads) *cthreads = d.cthreads;
   return EA_OK;
@@ -2485,7 +2586,7 @@ int ea_sp_job_bytes(const ea_sp_geom *gp, const ea_cadence *cad, const double *b
   const uint64_t V = g.V, NB = gp->nbetas, NR = gp->nrep, nw = gp->nwords, G = NR * NB;
   add(V * 24); add(V * 4);                                   // neighbour table, colour lists
   add(nw * V * G * 8); add(nw * V * 48);                     // spins, couplings
-  add(NB * 256 * 8); add(NB * 256 * 2);                      // thresholds, pre-search
+  add(NB * 256 * 8); add(NB * 256 * 2); add(NB * kPre11Stride);  // thresholds, pre-searches
   add(NR * 16); add(NR * 4); add(NR * sizeof(ea_hq)); add(NR * sizeof(ea_xoshiro)); add(8);
   add(nw * 64 * G * 4); add(nw * 64 * G * 4); add(nw * 64 * G);   // U2, E, slot permutations
   add(nw * 64 * NR * (NB - 1) * 4); add(nw * NR * (NB - 1) * 8); // accepted swaps, lane masks

@@ -41,6 +41,7 @@ struct SpDev {
   int echunk;                        // sites per thread of the energy count
   int esites, epair;                 // sites the count walks: all V, or (epair = 1) the colour-1 sites, counted twice
   int cthreads;                      // block size of the one-job cluster labelling
+  int pgrid;                         // > 0: one-job colour passes as the per-item pass on this many CTAs
   int col_off[9];                    // colour c owns col_sites[col_off[c] .. col_off[c+1])
   const int32_t *nb;                 // [V][6]
   const int32_t *col_sites;          // [V]
@@ -48,6 +49,7 @@ struct SpDev {
   const unsigned long long *J;       // [nw][V][6] coupling words
   const unsigned long long *cum;     // [NB][256] thresholds
   const uint16_t *pre;               // [NB][256] 8-bit pre-search
+  const uint8_t *pre11;              // [NB][2064] 11-bit pre-search (the per-item pass)
   uint4 *ctr;                        // [NR] Philox counters of the current pass
   const uint32_t *keys;              // [NR]
   ea_hq *prc;                        // [NR]
@@ -92,6 +94,8 @@ int sp_kt(int NB, int NR, int nsites_colour);
 int sp_slab_planes(int L, int Lz, int nw, int nclust);
 int sp_energy_chunk(const SpDev &d);
 size_t sp_sweep_smem(int NB, int NR, int kt);
+size_t sp_items_smem(int NB);
+int sp_items_grid(int NB);
 cudaError_t sp_setup();
 cudaError_t sp_launch_pass(const SpDev &d, int colour, int off, int n, cudaStream_t st);
 cudaError_t sp_launch_energy(const SpDev &d, cudaStream_t st);

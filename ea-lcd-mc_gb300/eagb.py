@@ -546,8 +546,13 @@ class SpJob:
         _ck(lib().ea_sp_plane_correlations(self.h, int(nrep), int(dmax), P(out)))
         return out
 
+    def set_tile(self, tile):
+        """ea_sp_set_tile: colour passes in tiles of `tile` sites, or 0 for the per-item pass."""
+        _ck(lib().ea_sp_set_tile(self.h, int(tile)))
+
     def autotune(self):
-        """ea_sp_autotune: (tile width, energy sites per thread, labelling block size) chosen."""
+        """ea_sp_autotune: (tile width -- 0 for the per-item pass --, energy sites
+        per thread, labelling block size) chosen."""
         kt, ec, ct = C.c_int32(), C.c_int32(), C.c_int32()
         _ck(lib().ea_sp_autotune(self.h, C.byref(kt), C.byref(ec), C.byref(ct)))
         return kt.value, ec.value, ct.value

@@ -390,12 +390,19 @@ int ea_sp_set_bin_kernel(ea_sp *job, int32_t mode);
  * takes for a bin of this cadence. */
 int ea_sp_bin_kernel_for(ea_sp *job, const ea_cadence *cad, int32_t *mode);
 /* Autotuner (no reference counterpart): times, on the job itself, the launch
- * shapes that leave every result unchanged -- the colour pass's tile width,
- * the energy count's sites per thread and the cluster labelling's block size
- * -- and keeps the fastest of each; the job's state is saved on the device
- * and put back, so its results are those of the untuned job.  Allocates the
- * overlap buffer of the cluster moves if it is missing.  Outputs may be NULL. */
+ * shapes that leave every result unchanged -- the colour pass's form (tiles
+ * of `tile` sites staging their random words in SMEM, or tile 0: the
+ * per-item pass, one thread per (site, replica, slot) drawing its own words
+ * on a grid of resident CTAs), the energy count's sites per thread and the
+ * cluster labelling's block size -- and keeps the fastest of each; the job's
+ * state is saved on the device and put back, so its results are those of the
+ * untuned job.  Allocates the overlap buffer of the cluster moves if it is
+ * missing.  Outputs may be NULL. */
 int ea_sp_autotune(ea_sp *job, int32_t *tile, int32_t *echunk, int32_t *cthreads);
+/* Sets the colour pass's form by hand: tile > 0 sites per CTA (1..64, the
+ * CTA's tables fitting in SMEM), or 0 for the per-item pass.  The words are
+ * the same in every form.  ea_sp_info reports the form in force. */
+int ea_sp_set_tile(ea_sp *job, int32_t tile);
 /* Configuration analysis of the job's current spins (no reference code; the
  * reference's DATA/README.md describes correlation functions of the overlap
  * built from f, g in {x, x^3, sign x} with r = 2, 4, 6, 8 replicas).  The

@@ -243,9 +243,16 @@ CASES = [(6, 8, eagb.EA_PBC, "T08_16_N4", 2, 2), (5, 7, eagb.EA_OBC, "T07_16_N6"
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("tile", [None, 0, 4])
 @pytest.mark.parametrize("L,Lz,bc,ln,NR,nw", CASES)
-def test_sweeps_energy_tempering_match_oracle(L, Lz, bc, ln, NR, nw):
+def test_sweeps_energy_tempering_match_oracle(L, Lz, bc, ln, NR, nw, tile):
+    """tile None: the job's default form (the per-item pass for one word,
+    tiles for more); 0: the per-item pass (one thread per site, replica and
+    slot); 4: tiles of 4 sites staging their random words in SMEM."""
     job = new_job(L, Lz, bc, ln, NR, nw)
+    if tile is not None:
+        job.set_tile(tile)
+        assert job.info()[1] == tile
     orc = OracleSP(job, 3)
     job.sweeps(2)
     orc.sweeps(2)
@@ -441,18 +448,24 @@ def oracle_bin(orc, itmax, houfr, mesfr, ptfr, cluster, nclust=0):
 # the 16-byte two-slot pass, the tile width, the energy chunking and the
 # 4-samples-per-pass labelling of 6912-site lattices as the bench runs them;
 # and the large tube as written (L=24, Lz=192, OBC, NT=32 in [0.6, 1.6],
-# NR=4, one word, a move every 5 sweeps): labelling in global scratch
-TIMED = [(6, 24, eagb.EA_PBC, "T08_16_N12", 2, 1, (512, 1, 1, 1, False)),
-         (12, 48, eagb.EA_OBC, "T07_16_N24", 4, 1, (10, 10, 1, 1, True)),
-         (12, 48, eagb.EA_OBC, "T07_16_N24", 4, 64, (1, 10, 1, 1, True)),
-         (24, 192, eagb.EA_OBC, "T06_16_N32", 4, 1, (1, 5, 1, 1, True))]
+# NR=4, one word, a move every 5 sweeps): slab labelling.  One-word jobs
+# take the per-item pass by default; they also run with the tiles their
+# heuristic chooses (8 and 32 sites).
+TIMED = [(6, 24, eagb.EA_PBC, "T08_16_N12", 2, 1, (512, 1, 1, 1, False), None),
+         (12, 48, eagb.EA_OBC, "T07_16_N24", 4, 1, (10, 10, 1, 1, True), None),
+         (12, 48, eagb.EA_OBC, "T07_16_N24", 4, 1, (10, 10, 1, 1, True), 8),
+         (12, 48, eagb.EA_OBC, "T07_16_N24", 4, 64, (1, 10, 1, 1, True), None),
+         (24, 192, eagb.EA_OBC, "T06_16_N32", 4, 1, (1, 5, 1, 1, True), None),
+         (24, 192, eagb.EA_OBC, "T06_16_N32", 4, 1, (1, 5, 1, 1, True), 32)]
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("L,Lz,bc,ln,NR,nw,cad", TIMED)
-def test_timed_configurations_match_oracle(L, Lz, bc, ln, NR, nw, cad):
+@pytest.mark.parametrize("L,Lz,bc,ln,NR,nw,cad,tile", TIMED)
+def test_timed_configurations_match_oracle(L, Lz, bc, ln, NR, nw, cad, tile):
     itmax, houfr, mesfr, ptfr, cl = cad
     job = new_job(L, Lz, bc, ln, NR, nw, jobid=0)
+    if tile is not None:
+        job.set_tile(tile)
     orc = OracleSP(job, 0)
     avg = job.run_bin(itmax, houfr, mesfr, ptfr, cluster=cl, nclust=0)
     want = oracle_bin(orc, itmax, houfr, mesfr, ptfr, cl)
@@ -559,7 +572,7 @@ def test_autotuned_job_equals_untuned(L, Lz, bc, ln, NR, nw):
     b.set_bin_kernel(eagb.EA_BIN_GRAPH)
     S0, c0 = b.get_spins(), b.counter()
     kt, ec, ct = b.autotune()
-    assert kt >= 1 and ec >= 1 and ct in (256, 512, 1024)
+    assert kt >= 0 and ec >= 1 and ct in (256, 512, 1024)
     assert np.array_equal(b.get_spins(), S0) and b.counter() == c0
     orc = OracleSP(a, 15)
     for cl in (True, False):
