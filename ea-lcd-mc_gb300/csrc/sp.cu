@@ -1562,6 +1562,13 @@ int ea_sp_host_init(const ea_sp_geom *gp, uint64_t seed_J, uint64_t seed_u, uint
   return EA_OK;
 }
 
+int ea_sp_presearch11(const uint64_t *cum, uint8_t *pre) {
+  if (!cum || !pre) return spfail(EA_ERR_ARG, "null argument");
+  if (cum[255] != ~0ULL) return spfail(EA_ERR_ARG, "threshold 255 is not 2^64-1");
+  presearch11(cum, pre);
+  return EA_OK;
+}
+
 int ea_sp_create(const ea_sp_geom *gp, int32_t device, ea_sp **out) {
   if (!gp || !out) return spfail(EA_ERR_ARG, "null argument");
   if (!geom_ok(gp)) return spfail(EA_ERR_ARG, "2 <= nbetas <= 64, 1 <= nrep <= 64, nwords >= 1");

@@ -490,6 +490,15 @@ def sp_host_init(g, seed_J, seed_u):
     return J, S
 
 
+def sp_presearch11(cum):
+    """ea_sp_presearch11: the per-item pass's 11-bit pre-search of one
+    temperature's thresholds (2064 bytes)."""
+    c = np.ascontiguousarray(cum, np.uint64)
+    pre = np.zeros(2064, np.uint8)
+    _ck(lib().ea_sp_presearch11(P(c), P(pre)))
+    return pre
+
+
 class SpJob:
     """A sample-packed job (ea_sp): 64 * nwords samples of an L x L x Lz tube."""
 

@@ -321,6 +321,12 @@ typedef struct ea_sp ea_sp;
 int ea_sp_graph(int32_t L, int32_t Lz, int32_t bc, int32_t *nb, int32_t *mate, uint8_t *colour, int32_t *ncol);
 /* Couplings and initial spins as ea_sp_init makes them (host only). */
 int ea_sp_host_init(const ea_sp_geom *g, uint64_t seed_J, uint64_t seed_u, uint64_t *J, uint64_t *S);
+/* The 11-bit pre-search table of one temperature's 256 thresholds, as the
+ * per-item colour pass stages it (host only; no reference counterpart):
+ * pre[t] = the first byte n with (t << 53) < cum[n] for t < 2048, and 255
+ * for t = 2048..2063.  The byte of a key R lies in [pre[R >> 53],
+ * pre[(R >> 53) + 1]].  cum[255] must be 2^64-1. */
+int ea_sp_presearch11(const uint64_t *cum, uint8_t *pre);
 int ea_sp_create(const ea_sp_geom *g, int32_t device, ea_sp **out);
 int ea_sp_destroy(ea_sp *job);
 int ea_sp_info(const ea_sp *job, int32_t *ncol, int32_t *tile);

@@ -89,6 +89,34 @@ def test_colour_counts_all_small_tubes():
                 assert np.all(col[nb] != col[:, None])
 
 
+@pytest.mark.parametrize("ln", ["T06_16_N32", "T07_16_N24", "T08_16_N12"])
+def test_presearch11_brackets_every_key(ln):
+    """The 11-bit pre-search of the per-item pass: entry t is the byte of
+    the bucket's smallest key (the first n with key < cum[n]), the padding
+    is 255, and every key's byte lies between its bucket's entry and the
+    next one -- at the bucket edges and for random keys."""
+    betas, cum = lut(ln)
+    rng = np.random.default_rng(5)
+
+    def byte(R):  # the reference's search: first n with R < cum[n], at most 255
+        return np.minimum(np.searchsorted(c, R, side="right"), 255)
+
+    for c in np.asarray(cum, np.uint64)[::7]:
+        pre = eagb.sp_presearch11(c)
+        edges = np.arange(2048, dtype=np.uint64) << np.uint64(53)
+        assert np.array_equal(pre[:2048], byte(edges))
+        assert np.all(pre[2048:] == 255)
+        R = np.concatenate([rng.integers(0, 2**64, 200000, dtype=np.uint64, endpoint=False),
+                            edges, edges + np.uint64((1 << 53) - 1), c[:255], c[:255] - np.uint64(1)])
+        t = (R >> np.uint64(53)).astype(np.int64)
+        b = byte(R)
+        assert np.all(pre[t] <= b) and np.all(b <= pre[t + 1])
+    with pytest.raises(RuntimeError):
+        bad = np.array(c, np.uint64)
+        bad[255] = 1
+        eagb.sp_presearch11(bad)
+
+
 def test_couplings_and_spins():
     g = eagb.SpGeom(5, 7, 4, 3, 2, eagb.EA_OBC)
     nb, mate, col, ncol = eagb.sp_graph(5, 7, eagb.EA_OBC)
