@@ -238,6 +238,15 @@ CPU_SAMPLE = ("31 samples x the full step of the GPU arm (5 sweeps with energy a
               "move with host cuRAND uniforms, the energy measurement), oracle C restatement, OpenMP")
 
 
+def max_over_ranks(torch, vals, device, world):
+    """Each timing as the slowest rank saw it (every rank runs its own
+    replica; whole-job throughput = all ranks' work / this time)."""
+    t = torch.tensor(vals, dtype=torch.float64, device=device)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -948,11 +957,7 @@ def run_ours(args, rank, world, local):
     e2e_serial_s, _ = run_e2e(False)
     e2e_s, e2e_steps = run_e2e(True)
 
-    # max over ranks
-    t = torch.tensor([ms, e2e_s, e2e_serial_s], dtype=torch.float64, device=dev)
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    ms, e2e_s, e2e_serial_s = float(t[0]), float(t[1]), float(t[2])
+    ms, e2e_s, e2e_serial_s = max_over_ranks(torch, [ms, e2e_s, e2e_serial_s], dev, world)
     if rank != 0:
         job.close()
         return
