@@ -153,6 +153,74 @@ __device__ __forceinline__ void sp_pass_body(const SpDev &d, int off, int n, int
   }
 }
 
+// One colour pass as a persistent grid of per-item threads: a thread takes
+// (site, replica, slot) items of the colour in turn -- consecutive lanes on
+// consecutive slots, so a warp's loads and stores cover consecutive words --
+// draws the item's three random words and updates the item's word in each
+// sample word.  Each CTA stages the 11-bit pre-search tables once (the
+// thresholds, rarely read past them, come through the read-only cache); no
+// random word goes through SMEM and no barrier separates drawing from
+// updating.  Same words as k_sp_pass (same random words per (slot, site,
+// replica), same flip mask): this form suits jobs with few sample words,
+// whose staged tiles spend their time on barriers and SMEM traffic for words
+// used once.
+// Items [t0, tend) of the colour's n x NR x NB, a thread from t0 with the
+// given stride (the calling block's threads take consecutive t0).
+__device__ __forceinline__ void sp_pass_items_body(const SpDev &d, int off, int n, long long t0, long long tend,
+                                                   long long stride, unsigned char *smem) {
+  const int NB = d.NB, NR = d.NR, G = NR * NB, V = d.V;
+  uint8_t *s_pre = smem;
+  {
+    const uint4 *ps = reinterpret_cast<const uint4 *>(d.pre11);
+    uint4 *pd = reinterpret_cast<uint4 *>(s_pre);
+    for (int i = threadIdx.x; i < NB * (kPre11Stride / 16); i += blockDim.x) pd[i] = ps[i];
+  }
+  __syncthreads();
+  const long long t1 = min(tend, (long long)n * G);
+  const size_t wps = (size_t)V * G;  // words per sample word
+  for (long long t = t0; t < t1; t += stride) {
+    const int b = (int)(t % NB), r = (int)((t / NB) % NR), k = (int)(t / G);
+    const int site = __ldg(d.col_sites + off + k);
+    const uint32_t tp = (uint32_t)(((size_t)b * V + site) * NR + r);
+    const uint4 c = d.ctr[r];
+    const uint32_t key = __ldg(d.keys + r);
+    const u64 *cum = d.cum + b * 256;
+    const uint8_t *pre = s_pre + b * kPre11Stride;
+    uint32_t w[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q)
+      w[q] = rnd_word_by(c.x + q, c.y, c.z + tp, c.w, key, tp,
+                         [&](uint32_t hi, uint32_t lo) { return lut_byte11(hi, lo, cum, pre); });
+    const u64 r0 = ((u64)w[0] << 32) | w[1], r1 = ((u64)w[2] << 32) | w[3], r2 = ((u64)w[4] << 32) | w[5];
+    int nbr[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) nbr[q] = __ldg(d.nb + (size_t)site * 6 + q);
+    u64 *Sc = d.S + (size_t)r * NB + b;
+    for (int ww = 0; ww < d.nw; ++ww) {
+      u64 *Sw = Sc + (size_t)ww * wps;
+      const u64 *Jp = d.J + ((size_t)ww * V + site) * 6;
+      const u64 sv = Sw[(size_t)site * G];
+      u64 f[6];
+#pragma unroll
+      for (int q = 0; q < 6; ++q) f[q] = sv ^ __ldg(Jp + q) ^ Sw[(size_t)nbr[q] * G];
+      Sw[(size_t)site * G] = sv ^ flip_mask(f, r0, r1, r2);
+    }
+  }
+}
+
+// A job's colour pass by its form; blk counts the job's blocks of the pass
+// (tiles, or kItemsPerThread x blockDim.x items of the per-item form).
+constexpr int kItemsPerThread = 4;
+__device__ __forceinline__ void sp_pass_any(const SpDev &d, int colour, int blk, unsigned char *smem) {
+  const int off = d.col_off[colour], n = d.col_off[colour + 1] - off;
+  if (d.pgrid) {
+    const long long t0 = (long long)blk * blockDim.x * kItemsPerThread;
+    sp_pass_items_body(d, off, n, t0 + threadIdx.x, t0 + (long long)blockDim.x * kItemsPerThread, blockDim.x, smem);
+  } else {
+    sp_pass_body(d, off, n, blk, smem);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Energy: per (word, sample, replica, slot) the number of unsatisfied
 // half-edges U2 (each bond counted from both ends), so E = 3V - U2
@@ -917,7 +985,7 @@ __global__ void kb_sp_fill(const __grid_constant__ SpBatchDev b, int colour) {
 __global__ void __launch_bounds__(512) kb_sp_pass(const __grid_constant__ SpBatchDev b, int colour) {
   extern __shared__ __align__(16) unsigned char smem[];
   SPB_ITEM(SPB_PASS0 + colour)
-  sp_pass_body(d, d.col_off[colour], d.col_off[colour + 1] - d.col_off[colour], blk, smem);
+  sp_pass_any(d, colour, blk, smem);
 }
 __global__ void kb_sp_zero(const __grid_constant__ SpBatchDev b) {
   SPB_ITEM(SPB_ZERO)
@@ -965,8 +1033,11 @@ size_t sp_cluster_smem(int V);
 void sp_batch_blocks(const SpDev &d, bool cluster, uint32_t out[SPB_COUNT]) {
   const long long G = (long long)d.NR * d.NB, nw = d.nw;
   for (int k = 0; k < SPB_COUNT; ++k) out[k] = 0;
-  for (int c = 0; c < kSpBatchMaxColours && c < d.ncol; ++c)
-    out[SPB_PASS0 + c] = (uint32_t)((d.col_off[c + 1] - d.col_off[c] + d.kt - 1) / d.kt);
+  for (int c = 0; c < kSpBatchMaxColours && c < d.ncol; ++c) {
+    const long long n = d.col_off[c + 1] - d.col_off[c];
+    out[SPB_PASS0 + c] = d.pgrid ? (uint32_t)((n * G + 512LL * kItemsPerThread - 1) / (512LL * kItemsPerThread))
+                                 : (uint32_t)((n + d.kt - 1) / d.kt);
+  }
   out[SPB_ZERO] = out[SPB_MEASURE] = (uint32_t)((nw * 64 * G + 255) / 256);
   out[SPB_ENERGY] = (uint32_t)((nw * ((d.esites + d.echunk - 1) / d.echunk) * G + 255) / 256);
   out[SPB_PT] = (uint32_t)(nw * d.NR);
@@ -1151,7 +1222,7 @@ __global__ void __launch_bounds__(kPersistThreads, 1) k_sp_persist(const __grid_
               if (c < s_job[0].ncol) sp_fill_body(s_job[0]);
             }
             SPP_SYNC();
-            SPP_BLOCKS(SPB_PASS0 + c, sp_pass_body(d, d.col_off[c], d.col_off[c + 1] - d.col_off[c], blk, smem))
+            SPP_BLOCKS(SPB_PASS0 + c, sp_pass_any(d, c, blk, smem))
             SPP_SYNC();
           }
         }
@@ -1232,57 +1303,10 @@ __global__ void __launch_bounds__(512) k_sp_pass(const __grid_constant__ SpDev d
   sp_pass_body(d, off, n, blockIdx.x, smem);
 }
 
-// One colour pass as a persistent grid of per-item threads: a thread takes
-// (site, replica, slot) items of the colour in turn -- consecutive lanes on
-// consecutive slots, so a warp's loads and stores cover consecutive words --
-// draws the item's three random words and updates the item's word in each
-// sample word.  Each CTA stages the 11-bit pre-search tables once (the
-// thresholds, rarely read past them, come through the read-only cache); no
-// random word goes through SMEM and no barrier separates drawing from
-// updating.  Same words as k_sp_pass (same random words per (slot, site,
-// replica), same flip mask): this form suits jobs with few sample words,
-// whose staged tiles spend their time on barriers and SMEM traffic for words
-// used once.
 __global__ void __launch_bounds__(512) k_sp_pass_items(const __grid_constant__ SpDev d, int off, int n) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int NB = d.NB, NR = d.NR, G = NR * NB, V = d.V;
-  uint8_t *s_pre = smem;
-  {
-    const uint4 *ps = reinterpret_cast<const uint4 *>(d.pre11);
-    uint4 *pd = reinterpret_cast<uint4 *>(s_pre);
-    for (int i = threadIdx.x; i < NB * (kPre11Stride / 16); i += blockDim.x) pd[i] = ps[i];
-  }
-  __syncthreads();
-  const long long total = (long long)n * G, stride = (long long)gridDim.x * blockDim.x;
-  const size_t wps = (size_t)V * G;  // words per sample word
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
-    const int b = (int)(t % NB), r = (int)((t / NB) % NR), k = (int)(t / G);
-    const int site = __ldg(d.col_sites + off + k);
-    const uint32_t tp = (uint32_t)(((size_t)b * V + site) * NR + r);
-    const uint4 c = d.ctr[r];
-    const uint32_t key = __ldg(d.keys + r);
-    const u64 *cum = d.cum + b * 256;
-    const uint8_t *pre = s_pre + b * kPre11Stride;
-    uint32_t w[6];
-#pragma unroll
-    for (int q = 0; q < 6; ++q)
-      w[q] = rnd_word_by(c.x + q, c.y, c.z + tp, c.w, key, tp,
-                         [&](uint32_t hi, uint32_t lo) { return lut_byte11(hi, lo, cum, pre); });
-    const u64 r0 = ((u64)w[0] << 32) | w[1], r1 = ((u64)w[2] << 32) | w[3], r2 = ((u64)w[4] << 32) | w[5];
-    int nbr[6];
-#pragma unroll
-    for (int q = 0; q < 6; ++q) nbr[q] = __ldg(d.nb + (size_t)site * 6 + q);
-    u64 *Sc = d.S + (size_t)r * NB + b;
-    for (int ww = 0; ww < d.nw; ++ww) {
-      u64 *Sw = Sc + (size_t)ww * wps;
-      const u64 *Jp = d.J + ((size_t)ww * V + site) * 6;
-      const u64 sv = Sw[(size_t)site * G];
-      u64 f[6];
-#pragma unroll
-      for (int q = 0; q < 6; ++q) f[q] = sv ^ __ldg(Jp + q) ^ Sw[(size_t)nbr[q] * G];
-      Sw[(size_t)site * G] = sv ^ flip_mask(f, r0, r1, r2);
-    }
-  }
+  sp_pass_items_body(d, off, n, (long long)blockIdx.x * blockDim.x + threadIdx.x, (long long)n * d.NR * d.NB,
+                     (long long)gridDim.x * blockDim.x, smem);
 }
 __global__ void __launch_bounds__(256) k_sp_energy(const __grid_constant__ SpDev d) {
   sp_energy_body(d, (long long)blockIdx.x * blockDim.x + threadIdx.x);
@@ -2369,7 +2393,8 @@ static int spb_upload(SpClass &k, bool cluster, cudaStream_t bs) {
     uint32_t cnt[SPB_COUNT];
     sp_batch_blocks(hj[i], cluster, cnt);
     for (int q = 0; q < SPB_COUNT; ++q) hp[(size_t)q * (n + 1) + i + 1] = hp[(size_t)q * (n + 1) + i] + cnt[q];
-    pass_smem = std::max(pass_smem, (int)sp_sweep_smem(hj[i].NB, hj[i].NR, hj[i].kt));
+    pass_smem = std::max(pass_smem, (int)(hj[i].pgrid ? sp_items_smem(hj[i].NB)
+                                                       : sp_sweep_smem(hj[i].NB, hj[i].NR, hj[i].kt)));
     perm_smem = std::max(perm_smem, kPermRows * (hj[i].NB | 1) * 8);
     if (cluster) cl_smem = std::max(cl_smem, (int)sp_cluster_smem(hj[i].V));
   }
