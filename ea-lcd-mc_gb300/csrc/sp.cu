@@ -153,19 +153,20 @@ __device__ __forceinline__ void sp_pass_body(const SpDev &d, int off, int n, int
   }
 }
 
-// One colour pass as a persistent grid of per-item threads: a thread takes
-// (site, replica, slot) items of the colour in turn -- consecutive lanes on
-// consecutive slots, so a warp's loads and stores cover consecutive words --
-// draws the item's three random words and updates the item's word in each
-// sample word.  Each CTA stages the 11-bit pre-search tables once (the
-// thresholds, rarely read past them, come through the read-only cache); no
-// random word goes through SMEM and no barrier separates drawing from
-// updating.  Same words as k_sp_pass (same random words per (slot, site,
-// replica), same flip mask): this form suits jobs with few sample words,
-// whose staged tiles spend their time on barriers and SMEM traffic for words
-// used once.
-// Items [t0, tend) of the colour's n x NR x NB, a thread from t0 with the
-// given stride (the calling block's threads take consecutive t0).
+// The per-item form of a colour pass.  A thread takes (site, replica, slot)
+// items of the colour in turn -- consecutive lanes on consecutive slots, so a
+// warp's loads and stores cover consecutive words -- draws the item's three
+// random words and updates the item's word in each sample word.  The block
+// stages the 11-bit pre-search tables once (the thresholds, rarely read past
+// them, come through the read-only cache); no random word goes through SMEM
+// and no barrier separates drawing from updating.  The words are those of the
+// tiles (same random words per (slot, site, replica), same flip mask).  This
+// form suits jobs with few sample words, whose tiles spend their time on
+// barriers and SMEM traffic for random words used once.
+// The thread takes items t0, t0 + stride, ... below tend of the colour's
+// n x NR x NB (the block's threads take consecutive t0): one job runs it on
+// a grid of resident CTAs (k_sp_pass_items), a batch on 4 x 512 items a
+// block (sp_pass_any).
 __device__ __forceinline__ void sp_pass_items_body(const SpDev &d, int off, int n, long long t0, long long tend,
                                                    long long stride, unsigned char *smem) {
   const int NB = d.NB, NR = d.NR, G = NR * NB, V = d.V;
