@@ -96,6 +96,8 @@ def correlation_observables(C, nblocks=10):
     the jackknife over `nblocks` consecutive blocks of samples."""
     C = np.asarray(C, np.float64)
     ns = C.shape[0]
+    if ns < 2:
+        raise ValueError("the jackknife needs at least 2 samples, got %d" % ns)
     nb = max(2, min(nblocks, ns))
     edges = np.linspace(0, ns, nb + 1).astype(int)
     sums = np.stack([C[edges[i]:edges[i + 1]].sum(0) for i in range(nb)])

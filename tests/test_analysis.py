@@ -45,6 +45,19 @@ def test_observables_and_jackknife():
     assert np.isclose(obs["C_Q_Q3"][1][1, 2], err)
 
 
+def test_jackknife_block_edges():
+    """Fewer samples than blocks: one sample a block (the plain jackknife);
+    a single sample has no error estimate and is refused."""
+    rng = np.random.default_rng(6)
+    C = rng.normal(size=(3, 1, 2, 3, 3))
+    obs = analysis.correlation_observables(C, nblocks=10)
+    x = C[:, 0, 1, 0, 2]
+    jk = (x.sum() - x) / 2
+    assert np.isclose(obs["C_Q_signQ"][1][0, 1], np.sqrt(2 / 3 * ((jk - jk.mean()) ** 2).sum()))
+    with pytest.raises(ValueError):
+        analysis.correlation_observables(C[:1])
+
+
 def test_data_file_layout(tmp_path):
     rng = np.random.default_rng(4)
     C = rng.normal(size=(16, 2, 3, 3, 3))
