@@ -407,7 +407,9 @@ int ea_sp_bin_kernel_for(ea_sp *job, const ea_cadence *cad, int32_t *mode);
 int ea_sp_autotune(ea_sp *job, int32_t *tile, int32_t *echunk, int32_t *cthreads);
 /* Sets the colour pass's form by hand: tile > 0 sites per CTA (1..64, the
  * CTA's tables fitting in SMEM), or 0 for the per-item pass.  The words are
- * the same in every form.  ea_sp_info reports the form in force. */
+ * the same in every form.  A job starts with the per-item pass if it has one
+ * sample word, else with tiles of a heuristic width; batches run each job's
+ * form.  ea_sp_info reports the form in force. */
 int ea_sp_set_tile(ea_sp *job, int32_t tile);
 /* Configuration analysis of the job's current spins (no reference code; the
  * reference's DATA/README.md describes correlation functions of the overlap
